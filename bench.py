@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Throughput of the FFT3D block-FFT denoise path on GB300.
+
+Workload: 3840x2160 10-bit luma, sigma=3 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4
+precision=2, a seeded synthetic 48-frame clip (ramp + moving rectangles in
+64..940, Gaussian noise 12 LSB). One step is one output frame in steady
+state: the forward transform of the frame that enters the temporal window,
+then filter + inverse + overlap-add + 10-bit packing of the current frame.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form exact|fast|tc]
+    python bench.py --impl reference ...   # the reference CPU path on the host cores
+
+Prints one JSON line (rank 0). `value` is device throughput with the clip
+resident in HBM; `e2e` is the same metric through the C ABI with host
+buffers (host->device upload of the new frame and device->host readback of
+the output inside the timed region). For N > 1 each rank runs an independent
+replica on its own GPU (the path does not shard across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "4K 10-bit frames/s (bt=4,bw=32) plain vs batched-TC; p99 frame latency @16 streams"
+UNIT = "frames/s"
+W, H, BITS, NFRAMES = 3840, 2160, 10, 48
+PARAMS = dict(sigma=3.0, bt=4, bw=32, bh=32, ow=16, oh=16, sharpen=0.4, precision=2)
+WORKLOAD = ("3840x2160 YUV420P10 luma, sigma=3 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4 precision=2, "
+            "48-frame seeded clip, one output frame per step")
+
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant
+# kernel from one ncu capture, keyed by form; None until captured.
+NCU_TRAFFIC = {}
+
+
+def algorithmic_bytes(nb: int, fbw: int, bh: int, bt: int) -> dict:
+    """Bytes one output frame must move with resident spectra: the raw plane
+    in, the packed plane out, the new frame's spectrum written once and the
+    bt window spectra read once. Intermediates (filtered spectra, inverse
+    blocks) do not count."""
+    plane = W * H * 2
+    spec = nb * fbw * bh * 8
+    return {"plane": plane, "spectrum": spec, "frame": 2 * plane + spec * (1 + bt),
+            "filter_inverse": spec * bt}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_clip():
+    from fft3dcl_gb300 import synth
+    return synth.clip_yuv420p10_luma(W, H, NFRAMES)
+
+
+# --------------------------------------------------------------- CPU leg --
+
+def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_steps: int = 1):
+    """Oracle (the C restatement of the reference CPU backend) in steady
+    state: per step one new frame is uploaded and transformed, then the
+    window is filtered, inverted, overlap-added and downloaded. Returns
+    (frames/s, steps)."""
+    import ctypes as C
+    import oracle
+    L = oracle.lib()
+    pl = oracle.Plane(W, H, BITS, **PARAMS)
+    pl.build_degrid()
+    n = pl.nb * pl.fbw * pl.ip.bh
+    bt, cur = pl.ip.bt, pl.ip.current
+    slots = [(np.empty(n, np.float32), np.empty(n, np.float32)) for _ in range(bt + 1)]
+    plane = np.empty((H, W), np.float32)
+    out = np.empty((H, W), np.float32)
+    dst = np.empty((H, W), np.uint16)
+
+    def spectra(fn, slot):
+        f = frames[fn % len(frames)]
+        L.orc_upload(pl.h, oracle._ptr(f), f.strides[0], oracle._ptr(plane))
+        L.orc_compute_spectra(pl.h, oracle._ptr(plane), oracle._ptr(slot[0]), oracle._ptr(slot[1]), threads)
+
+    def step(nout):
+        # window of output frame nout: nout-cur .. nout-cur+bt-1; the last is new
+        new = nout - cur + bt - 1
+        spectra(new, slots[new % (bt + 1)])
+        win = [slots[(nout - cur + i) % (bt + 1)] for i in range(bt)]
+        wr = (C.c_void_p * bt)(*[w[0].ctypes.data for w in win])
+        wi = (C.c_void_p * bt)(*[w[1].ctypes.data for w in win])
+        L.orc_filter_and_synthesize(pl.h, wr, wi, bt, oracle._ptr(out), threads)
+        L.orc_download(pl.h, oracle._ptr(out), oracle._ptr(dst), dst.strides[0])
+
+    base = cur + 10
+    for i in range(bt - 1):  # window warm-up, untimed
+        spectra(base - cur + i, slots[(base - cur + i) % (bt + 1)])
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps and (steps < min_steps or time.perf_counter() - t0 < budget_s):
+        step(base + steps)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return steps / dt, steps
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path on the host cores. The
+    reference sources compile only here, so on the GPU host this is the C
+    restatement (oracle/), bit-identical to the reference by its tests."""
+    import oracle
+    oracle.build(ref=False)
+    frames = make_clip()
+    threads = os.cpu_count() or 1
+    fps_warm, _ = cpu_steady_state(frames, threads, 0.0, max(1, args.warmup), max(1, args.warmup))
+    fps, steps = cpu_steady_state(frames, threads, 0.0, args.steps, args.steps)
+    kind = "port"
+    line = {"metric": METRIC, "value": round(fps, 4), "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000.0 / fps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cpu_threads": threads},
+            "cpu_baseline": {"value": round(fps, 4), "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{steps} steady-state 4K output frames, all {threads} host threads, "
+                                       "C restatement of src/cpu (bit-identical to the reference)"},
+            "e2e": {"value": round(fps, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- GPU leg --
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    import fft3dcl_gb300 as F
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    frames = make_clip()
+    clip_dev = torch.from_numpy(np.stack(frames)).to(dev)  # [48, H, W] uint16, resident
+    stream = torch.cuda.Stream(device=dev)
+    eng = F.Engine(W, H, BITS, form=args.form, device=local_rank, stream=stream.cuda_stream, **PARAMS)
+    info = eng.info()
+    ip = F.validate(W, H, BITS, **PARAMS)
+    bt, cur = ip.bt, ip.current
+    pitch = W * 2
+    out = torch.empty((H, W), dtype=torch.uint16, device=dev)
+    nfr = clip_dev.shape[0]
+
+    def step(n):
+        win = [n - cur + i for i in range(bt)]
+        for fn in win:
+            if not eng.has(fn):
+                eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
+        eng.process_device(win, out.data_ptr(), pitch)
+        eng.prune(n - cur - 1, n - cur + bt)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    n = cur
+    for _ in range(max(3, args.warmup)):
+        step(n)
+        n += 1
+    torch.cuda.synchronize(dev)
+
+    clocks = Clocks(local_rank)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize(dev)
+    l0 = F.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(n)
+        n += 1
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    launches = F.kernel_launches() - l0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+
+    # Per-kernel device time over the same number of steps (a synchronize
+    # after each step so that the engine's events can be read).
+    kt = np.zeros(3)
+    for _ in range(args.steps):
+        step(n)
+        n += 1
+        eng.synchronize()
+        kt += np.array(eng.last_kernel_ms())
+    kt /= args.steps
+
+    # End to end through the C ABI with host buffers: pinned source planes,
+    # upload of the entering frame and readback of the packed output.
+    host = [torch.from_numpy(frames[i]).pin_memory() for i in range(min(8, nfr))]
+    hout = torch.empty((H, W), dtype=torch.uint16).pin_memory()
+    hnp = [h.numpy() for h in host]
+    hout_np = hout.numpy()
+    eng.prune(-1, -2)
+
+    def step_host(n):
+        win = [n - cur + i for i in range(bt)]
+        for fn in win:
+            if not eng.has(fn):
+                eng.forward_raw(fn, hnp[fn % len(hnp)])
+        eng.process_raw(win, hout_np)
+        eng.prune(n - cur - 1, n - cur + bt)
+
+    for _ in range(max(3, args.warmup)):
+        step_host(n)
+        n += 1
+    barrier()
+    torch.cuda.synchronize(dev)
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host(n)
+        n += 1
+    h1.record(stream)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    barrier()
+    ms_e2e = max(h0.elapsed_time(h1), wall * 1000.0)
+    eng.close()
+
+    if world > 1:
+        t = torch.tensor([ms, ms_e2e], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, ms_e2e = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    fps = args.steps * world / (ms / 1000.0)
+    fps_e2e = args.steps * world / (ms_e2e / 1000.0)
+    ab = algorithmic_bytes(info.nblocks, info.fbw, ip.bh, bt)
+    peak, peak_kind = load_peaks()
+    inv_ms = float(kt[1])
+    achieved = ab["filter_inverse"] / (inv_ms / 1000.0) / 1e9 if inv_ms > 0 else None
+    line = {
+        "metric": METRIC, "value": round(fps, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ramp + moving rectangles, Gaussian noise 12 LSB, 10-bit)",
+        "config": {"workload": WORKLOAD, "form": args.form, "parallelism": f"replicas x{world}",
+                   "inputs": "clip resident in HBM (48 x 16.6 MB)",
+                   "l2": "working set per step ~750 MB: four 143 MB window spectra, larger than the 129 MB L2"},
+        "kernel_ms": {"forward": round(float(kt[0]), 4), "filter_inverse": inv_ms and round(inv_ms, 4),
+                      "overlap_add": round(float(kt[2]), 4)},
+        "roofline": {"kernel": "filter_inverse", "bound": "hbm",
+                     "achieved": achieved and round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": achieved and round(achieved / peak, 4),
+                     "traffic": NCU_TRAFFIC.get(args.form), "algorithmic_bytes": ab["filter_inverse"],
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "roofline_step": {"algorithmic_bytes": ab["frame"],
+                          "achieved": round(ab["frame"] * fps / world / 1e9, 1), "unit": "GB/s",
+                          "frac": round(ab["frame"] * fps / world / 1e9 / peak, 4)},
+        "e2e": {"value": round(fps_e2e, 3), "unit": UNIT, "h2d_bytes_per_step": W * H * 2,
+                "d2h_bytes_per_step": W * H * 2},
+        "gpu_launches": int(launches), "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu:
+        cpu_threads = os.cpu_count() or 1
+        fps_cpu, steps = cpu_steady_state(frames, cpu_threads, 12.0, 30)
+        fps_cpu1, steps1 = cpu_steady_state(frames, 1, 0.0, 1)
+        line["cpu_baseline"] = {
+            "value": round(fps_cpu, 4), "unit": UNIT, "cores": cpu_threads, "kind": "port",
+            "sample": f"{steps} steady-state 4K output frames on {cpu_threads} host threads "
+                      f"(1 thread: {fps_cpu1:.4f} frames/s over {steps1} frame), C restatement of "
+                      "src/cpu, bit-identical to the reference"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="exact", choices=["exact", "fast", "tc"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    try:
+        run_gpu(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

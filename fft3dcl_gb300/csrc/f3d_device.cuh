@@ -1,0 +1,303 @@
+// f3d_device.cuh -- device helpers shared by all kernel forms: block grid,
+// pixel formats, the per-bin temporal filter and the radix-2 transforms.
+//
+// The arithmetic is written with plain operators. The exact-form translation
+// units are compiled with --fmad=false and IEEE division and square root, so
+// every expression rounds exactly like the reference's fp32 CPU code
+// (src/cpu/reference.cpp) when it is written in the same order, which it is.
+#pragma once
+
+#include "f3d_kernels.hpp"
+#include "fft3d_gb300.h"
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace f3d {
+
+template <int N>
+struct Log2 {
+  static constexpr int v = 1 + Log2<N / 2>::v;
+};
+template <>
+struct Log2<1> {
+  static constexpr int v = 0;
+};
+
+__host__ __device__ constexpr int bit_reverse(int i, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; b++)
+    if (i & (1 << b)) r |= 1 << (bits - 1 - b);
+  return r;
+}
+
+// D3D9 MIRROR addressing, src/cpu/reference.cpp:10-17.
+__device__ __forceinline__ int mirror_i(int x, int w) {
+  int p = x % (2 * w);
+  if (p < 0) p += 2 * w;
+  if (p >= w) p = 2 * w - 1 - p;
+  return p;
+}
+
+// Top-left corner and synthesis parity of block b (src/cpu/reference.cpp:23-46).
+__device__ __forceinline__ void block_origin(const Geo& g, int b, int& bx, int& by, int& par) {
+  if (g.mode == 1) {
+    const int m = b / g.ncols, n = b - m * g.ncols;
+    bx = g.xoff + n * g.xstep;
+    by = g.yoff + m * g.ystep;
+    par = n & 1;
+  } else {
+    const int per = g.ncols * g.nrows;
+    const int grid = b >= per ? 1 : 0;
+    const int r = b - grid * per;
+    const int j = r / g.ncols, i = r - j * g.ncols;
+    bx = i * g.bw - (grid ? g.bw / 2 : 0);
+    by = j * g.bh - (grid ? g.bh / 2 : 0);
+    par = 0;
+  }
+}
+
+// Source sample to float, src/cpu/reference.cpp:82-105.
+__device__ __forceinline__ float load_sample(const uint8_t* row, int x, int fmt, float norm) {
+  if (fmt == FMT_U8) return (float)row[x] * (1.0f / 255.0f);
+  if (fmt == FMT_U16) return (float)reinterpret_cast<const uint16_t*>(row)[x] * norm;
+  return reinterpret_cast<const float*>(row)[x];
+}
+
+// Float to destination sample, src/cpu/reference.cpp:107-138. The product
+// and the +0.5 are rounded separately (no fused multiply-add), and the cast
+// truncates a non-negative value, i.e. floors it.
+__device__ __forceinline__ void store_sample(uint8_t* row, int x, float v, int fmt, float inv_norm,
+                                             float max_pix) {
+  if (fmt == FMT_U8) {
+    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+    row[x] = (uint8_t)__float2uint_rz(__fadd_rn(__fmul_rn(v, 255.0f), 0.5f));
+  } else if (fmt == FMT_U16) {
+    v = __fmul_rn(v, inv_norm);
+    v = v < max_pix ? v : max_pix;
+    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+    reinterpret_cast<uint16_t*>(row)[x] = (uint16_t)__float2uint_rz(__fadd_rn(__fmul_rn(v, 65535.0f), 0.5f));
+  } else {
+    reinterpret_cast<float*>(row)[x] = v;
+  }
+}
+
+// Wiener shrink of one complex value, src/cpu/reference.cpp:201-209.
+__device__ __forceinline__ void wienner(float& re, float& im, float sx, float sy, float beta_x) {
+  float psd = re * re + im * im + 0.0000000000000000000000000000000000001f;
+  float psd_inv = 1.0f / psd;
+  float mul = beta_x;
+  if (1.0f / sx > psd_inv) mul = 1.0f - sy * psd_inv;
+  re *= mul;
+  im *= mul;
+}
+
+// Temporal filter + sharpen of bin i (0 <= i < bh*fbw) of block b, with
+// gi = b*bh*fbw + i. Follows src/cpu/reference.cpp:229-409 per bin:
+// degrid correction, bm 2/3/4 temporal DFT + Wiener, bm 1 Wiener, bm 0
+// Kalman (state updated in place), bm -1 pass-through, then sharpen.
+__device__ __forceinline__ float2 filter_bin(const InvArgs& a, int b, int i, size_t gi) {
+  float d_re = 0.0f, d_im = 0.0f;
+  if (a.dg) {
+    const size_t ps = (size_t)a.g.bh * a.g.fbw;
+    const float dc = a.s[a.cur][(size_t)b * ps].x;
+    const float2 g = a.gs[i];
+    d_re = dc * g.x;
+    d_im = dc * g.y;
+  }
+  float sx = a.sigma_x, sy = a.sigma_y;
+  if (a.pat) {
+    const float pv = a.pattern[i];
+    sx = pv * a.beta;
+    sy = pv;
+  }
+  float fr, fi;
+  const int bm = a.bm;
+  if (bm == 2) {
+    const float2 p = a.s[0][gi], c = a.s[1][gi];
+    float ar = c.x - p.x, ai = c.y - p.y;
+    float br = c.x + p.x, bi = c.y + p.y;
+    if (a.dg) {
+      br -= 2.0f * d_re;
+      bi -= 2.0f * d_im;
+    }
+    wienner(ar, ai, sx, sy, a.beta_x);
+    wienner(br, bi, sx, sy, a.beta_x);
+    fr = (ar + br) * 0.5f;
+    fi = (ai + bi) * 0.5f;
+    if (a.dg) {
+      fr += d_re;
+      fi += d_im;
+    }
+  } else if (bm == 3) {
+    const float2 p = a.s[0][gi], c = a.s[1][gi], n = a.s[2][gi];
+    const float K = 0.8660254f;  // truncated literal, src/cpu/reference.cpp:247
+    float t1r = p.x + n.x, t1i = p.y + n.y;
+    float y1r = c.x - 0.5f * t1r, y1i = c.y - 0.5f * t1i;
+    float dnr = n.x - p.x, dni = n.y - p.y;
+    float y2r = K * dni, y2i = -K * dnr;
+    float d0r = y1r + y2r, d0i = y1i + y2i;
+    float d1r = c.x + t1r, d1i = c.y + t1i;
+    float d2r = y1r - y2r, d2i = y1i - y2i;
+    if (a.dg) {
+      d1r -= 3.0f * d_re;
+      d1i -= 3.0f * d_im;
+    }
+    wienner(d0r, d0i, sx, sy, a.beta_x);
+    wienner(d1r, d1i, sx, sy, a.beta_x);
+    wienner(d2r, d2i, sx, sy, a.beta_x);
+    fr = (d0r + d1r + d2r) * (1.0f / 3.0f);
+    fi = (d0i + d1i + d2i) * (1.0f / 3.0f);
+    if (a.dg) {
+      fr += d_re;
+      fi += d_im;
+    }
+  } else if (bm == 4) {
+    const float2 p2 = a.s[0][gi], p1 = a.s[1][gi], c = a.s[2][gi], n = a.s[3][gi];
+    float fp1r = -p2.x + p1.y + c.x - n.y;
+    float fp1i = -p2.y - p1.x + c.y + n.x;
+    float fcr = p2.x + p1.x + c.x + n.x;
+    float fci = p2.y + p1.y + c.y + n.y;
+    float fnr = -p2.x - p1.y + c.x + n.y;
+    float fni = -p2.y + p1.x + c.y - n.x;
+    float fp2r = p2.x - p1.x + c.x - n.x;
+    float fp2i = p2.y - p1.y + c.y - n.y;
+    if (a.dg) {
+      fp1r -= 4.0f * d_re;
+      fp1i -= 4.0f * d_im;
+    }
+    wienner(fp2r, fp2i, sx, sy, a.beta_x);
+    wienner(fp1r, fp1i, sx, sy, a.beta_x);
+    wienner(fcr, fci, sx, sy, a.beta_x);
+    wienner(fnr, fni, sx, sy, a.beta_x);
+    fr = (fp2r + fp1r + fcr + fnr) * 0.25f;
+    fi = (fp2i + fp1i + fci + fni) * 0.25f;
+    if (a.dg) {
+      fr += d_re;
+      fi += d_im;
+    }
+  } else if (bm == 1) {
+    const float2 c = a.s[0][gi];
+    float re = c.x, im = c.y;
+    if (a.dg) {
+      re -= d_re;
+      im -= d_im;
+    }
+    wienner(re, im, sx, sy, a.beta_x);
+    if (a.dg) {
+      re += d_re;
+      im += d_im;
+    }
+    fr = re;
+    fi = im;
+  } else if (bm == 0) {
+    const float2 c = a.s[0][gi];
+    const float cn = a.pat ? a.pattern[i] : a.kalman_cn;
+    float2 l;
+    float s;
+    if (a.kalman_init) {  // src/cpu/reference.cpp:336-355: last = current, covar = proc = cn
+      l = c;
+      s = cn + cn;
+    } else {
+      l = a.klast[gi];
+      s = a.kcov[gi] + a.kproc[gi];
+    }
+    float dr = c.x - l.x, di = c.y - l.y;
+    float a2 = dr * dr, b2 = di * di;
+    float mask = a2 < b2 ? b2 : a2;  // std::max
+    float gain = s / (s + cn);
+    float new_proc = gain * gain * cn;
+    float new_covar = (1.0f - gain) * s;
+    float dst_r = gain * c.x + (1.0f - gain) * l.x;
+    float dst_i = gain * c.y + (1.0f - gain) * l.y;
+    if (mask > a.kr2 * cn) {
+      dst_r = c.x;
+      dst_i = c.y;
+      new_covar = cn;
+      new_proc = cn;
+    }
+    a.kcov[gi] = new_covar;
+    a.kproc[gi] = new_proc;
+    a.klast[gi] = make_float2(dst_r, dst_i);
+    fr = dst_r;
+    fi = dst_i;
+  } else {
+    const float2 c = a.s[0][gi];
+    fr = c.x;
+    fi = c.y;
+  }
+  if (a.shp) {  // src/cpu/reference.cpp:393-409
+    float re = fr, im = fi;
+    if (a.dg) {
+      re -= d_re;
+      im -= d_im;
+    }
+    float psd = re * re + im * im + 0.0000000000000000000000000000000000001f;
+    float factor = a.sharpen[i];
+    float g = 1.0f + factor * sqrtf(psd * a.ssmax / ((psd + a.ssmin) * (psd + a.ssmax)));
+    re *= g;
+    im *= g;
+    if (a.dg) {
+      re += d_re;
+      im += d_im;
+    }
+    fr = re;
+    fi = im;
+  }
+  return make_float2(fr, fi);
+}
+
+// One radix-2 DIT stage of length LEN over N register values: butterflies
+// (u + w*b, u - w*b) with twiddle tw[j * N/LEN], conjugated for the inverse.
+// The j = 0 twiddle is (1, -0) and its product equals b, so it is skipped.
+// Stages recurse at compile time so that every loop bound is a constant and
+// the array stays in registers.
+template <int N, int LEN, bool INV>
+__device__ __forceinline__ void fft_r2_stage(float2 (&a)[N], const float2* tw) {
+  constexpr int half = LEN / 2, step = N / LEN;
+#pragma unroll
+  for (int i = 0; i < N; i += LEN) {
+#pragma unroll
+    for (int j = 0; j < half; j++) {
+      const float2 b = a[i + j + half];
+      float2 t;
+      if (j == 0) {
+        t = b;
+      } else {
+        const float2 w = tw[j * step];
+        const float wy = INV ? -w.y : w.y;
+        t.x = w.x * b.x - wy * b.y;
+        t.y = w.x * b.y + wy * b.x;
+      }
+      const float2 u = a[i + j];
+      a[i + j] = make_float2(u.x + t.x, u.y + t.y);
+      a[i + j + half] = make_float2(u.x - t.x, u.y - t.y);
+    }
+  }
+  if constexpr (LEN < N) fft_r2_stage<N, LEN * 2, INV>(a, tw);
+}
+
+// Radix-2 decimation-in-time transform of N values held in registers, in the
+// operation order of the reference's FftPlan (src/cpu/fft.cpp:28-58): bit
+// reversal, stages len = 2..N, and for the inverse a final scale by 1/N.
+template <int N, bool INV>
+__device__ __forceinline__ void fft_r2(float2 (&a)[N], const float2* tw) {
+  constexpr int L = Log2<N>::v;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    const int r = bit_reverse(i, L);
+    if (i < r) {
+      const float2 t = a[i];
+      a[i] = a[r];
+      a[r] = t;
+    }
+  }
+  fft_r2_stage<N, 2, INV>(a, tw);
+  if (INV) {
+    const float invn = 1.0f / N;
+#pragma unroll
+    for (int i = 0; i < N; i++) a[i] = make_float2(a[i].x * invn, a[i].y * invn);
+  }
+}
+
+}  // namespace f3d

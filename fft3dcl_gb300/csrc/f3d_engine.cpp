@@ -1,0 +1,602 @@
+// f3d_engine.cpp -- the per-plane engine behind the C ABI (include/fft3d_gb300.h).
+//
+// Replaces the reference's OpenCL backend host class GpuRef
+// (src/cl/gpu.{h,cpp}). An engine owns, on one CUDA device and one stream:
+//   - the tables (windows, sigma pattern, sharpen LUT, degrid sample), built on
+//     the host exactly like the reference's CPU tables and uploaded once;
+//   - the spectra cache: one nb x bh x fbw complex buffer per cached frame,
+//     with the reference's reuse pool and 256 MiB retire budget;
+//   - the per-frame work buffers (raw plane in, windowed blocks, plane out);
+//   - the Kalman state for bt=0, resident across frames.
+// All device memory is counted in the process-wide live-bytes total.
+#include "f3d_host.hpp"
+#include "f3d_kernels.hpp"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace f3d {
+unsigned long long launch_count();
+}
+
+using namespace f3d;
+
+namespace {
+
+thread_local std::string t_last_error;
+std::atomic<int> g_live{0};
+std::atomic<size_t> g_bytes{0};
+
+int fail_thread(int code, const std::string& msg) {
+  t_last_error = msg;
+  return code;
+}
+
+}  // namespace
+
+struct f3d_engine {
+  std::mutex mtx;
+  std::string err;
+  f3d_internal_params ip{};
+  f3d_plane_geom geom{};
+  Grid grid;
+  int device = 0, form = F3D_FORM_EXACT;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int fbw = 0, ps = 0, bps = 1, fmt = FMT_U8;
+  float norm = 1.0f, inv_norm = 1.0f, max_pix = 0.0f, cnorm = 0.0f;
+  size_t spec_bytes = 0;
+
+  std::vector<float> win_ana, syn_a, syn_b, pattern, sharpen, gs, tw_row, tw_col;
+  float *d_win_ana = nullptr, *d_syn_a = nullptr, *d_syn_b = nullptr;
+  float *d_pattern = nullptr, *d_sharpen = nullptr;
+  float2* d_gs = nullptr;
+  bool degrid_active = false;
+
+  std::map<int, float2*> cache;
+  std::vector<float2*> pool;
+
+  uint8_t* d_in = nullptr;   // raw or float plane, width*height*4 bytes
+  uint8_t* d_out = nullptr;  // packed or float output plane
+  float* d_blocks = nullptr; // nb x bh x bw windowed blocks
+  float2* d_klast = nullptr;
+  float* d_kcov = nullptr;
+  float* d_kproc = nullptr;
+  bool kalman_first = true;
+
+  size_t bytes = 0;
+  // Kernel timing on the engine stream: forward [0,1], filter+inverse [2,4],
+  // overlap-add [4,3].
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool fwd_timed = false, proc_timed = false;
+
+  int fail(int code, const std::string& msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char* where) {
+    return fail(e == cudaErrorMemoryAllocation ? F3D_E_NOMEM : F3D_E_CUDA,
+                std::string("FFT3DCL: CUDA error at ") + where + ": " + cudaGetErrorString(e));
+  }
+  template <class T>
+  cudaError_t alloc(T** p, size_t n_bytes) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n_bytes);
+    if (e == cudaSuccess) {
+      bytes += n_bytes;
+      g_bytes += n_bytes;
+    } else {
+      *p = nullptr;
+      cudaGetLastError();
+    }
+    return e;
+  }
+  template <class T>
+  void release(T*& p, size_t n_bytes) {
+    if (p) {
+      cudaFree(p);
+      bytes -= n_bytes;
+      g_bytes -= n_bytes;
+      p = nullptr;
+    }
+  }
+};
+
+namespace {
+
+Geo make_geo(const f3d_engine* e) {
+  Geo g{};
+  g.W = e->geom.width;
+  g.H = e->geom.height;
+  g.bw = e->ip.bw;
+  g.bh = e->ip.bh;
+  g.fbw = e->fbw;
+  g.nb = e->grid.nb;
+  g.mode = e->grid.mode;
+  g.ncols = e->grid.ncols;
+  g.nrows = e->grid.nrows;
+  g.xoff = e->grid.xoff;
+  g.xstep = e->grid.xstep;
+  g.yoff = e->grid.yoff;
+  g.ystep = e->grid.ystep;
+  return g;
+}
+
+Twiddles make_twiddles(const f3d_engine* e) {
+  Twiddles t{};
+  for (int k = 0; k < e->ip.bw / 2; k++) t.row[k] = make_float2(e->tw_row[2 * k], e->tw_row[2 * k + 1]);
+  for (int k = 0; k < e->ip.bh / 2; k++) t.col[k] = make_float2(e->tw_col[2 * k], e->tw_col[2 * k + 1]);
+  return t;
+}
+
+// GpuRef::spectra (src/cl/gpu.cpp:272-287): cached buffer of frame fn, or a
+// recycled / new one.
+float2* spectra_slot(f3d_engine* e, int fn, bool create) {
+  auto it = e->cache.find(fn);
+  if (it != e->cache.end()) return it->second;
+  if (!create) return nullptr;
+  float2* m = nullptr;
+  if (!e->pool.empty()) {
+    m = e->pool.back();
+    e->pool.pop_back();
+  } else if (e->alloc(&m, e->spec_bytes) != cudaSuccess) {
+    return nullptr;
+  }
+  e->cache[fn] = m;
+  return m;
+}
+
+// GpuRef::retireSpectra (src/cl/gpu.cpp:289-306): keep recycled buffers up
+// to 256 MiB, release the rest.
+void retire(f3d_engine* e, float2* m) {
+  const size_t budget = size_t(256) << 20;
+  if (e->pool.size() * e->spec_bytes + e->spec_bytes <= budget)
+    e->pool.push_back(m);
+  else
+    e->release(m, e->spec_bytes);
+}
+
+int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int fmt) {
+  float2* spec = spectra_slot(e, fn, true);
+  if (!spec) return e->fail(F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
+  FwdArgs a{};
+  a.g = make_geo(e);
+  a.tw = make_twiddles(e);
+  a.src = dsrc;
+  a.pitch = pitch;
+  a.fmt = fmt;
+  a.norm = e->norm;
+  a.chroma_norm = e->cnorm;
+  a.win = e->d_win_ana;
+  a.spec = spec;
+  cudaEventRecord(e->ev[0], e->stream);
+  cudaError_t ce = launch_forward(e->form, a, e->stream);
+  cudaEventRecord(e->ev[1], e->stream);
+  e->fwd_timed = true;
+  if (ce != cudaSuccess) {
+    e->cache.erase(fn);
+    retire(e, spec);
+    return e->cuda_fail(ce, "the forward transform launch");
+  }
+  return F3D_OK;
+}
+
+int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long long pitch, int fmt) {
+  const int need = e->ip.bm >= 2 ? e->ip.bt : 1;
+  if (!window || n < need)
+    return e->fail(F3D_E_PARAM, "FFT3DCL: the window must hold " + std::to_string(need) + " frame(s)");
+  InvArgs a{};
+  for (int i = 0; i < 4; i++) {
+    const int fn = window[i < need ? i : 0];
+    const float2* s = spectra_slot(e, fn, false);
+    if (!s) return e->fail(F3D_E_STATE, "FFT3DCL: missing spectra in window (frame " + std::to_string(fn) + ")");
+    a.s[i] = s;
+  }
+  if (e->ip.degrid_on && !e->degrid_active) e->degrid_active = true;
+  a.g = make_geo(e);
+  a.tw = make_twiddles(e);
+  a.cur = e->ip.bm >= 2 ? e->ip.current : 0;
+  a.bm = e->ip.bm;
+  a.dg = e->ip.degrid_on && e->degrid_active;
+  a.pat = e->ip.use_pattern;
+  a.shp = e->ip.sharpen_on;
+  a.kalman_init = e->ip.bm == 0 && e->kalman_first;
+  a.gs = e->d_gs;
+  a.pattern = e->d_pattern;
+  a.sharpen = e->d_sharpen;
+  a.klast = e->d_klast;
+  a.kcov = e->d_kcov;
+  a.kproc = e->d_kproc;
+  a.win_a = e->grid.mode == 1 ? e->d_syn_a : e->d_win_ana;
+  a.win_b = e->grid.mode == 1 ? e->d_syn_b : e->d_win_ana;
+  a.blocks = e->d_blocks;
+  a.sigma_x = e->ip.beta * e->ip.wiener_s;
+  a.sigma_y = e->ip.wiener_s;
+  a.beta_x = e->ip.beta_x;
+  a.beta = e->ip.beta;
+  a.ssmin = e->ip.ssmin;
+  a.ssmax = e->ip.ssmax;
+  a.kalman_cn = e->ip.kalman_cn;
+  a.kr2 = e->ip.kratio * e->ip.kratio;
+  cudaEventRecord(e->ev[2], e->stream);
+  cudaError_t ce = launch_filter_inverse(e->form, a, e->stream);
+  cudaEventRecord(e->ev[4], e->stream);
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "the filter/inverse launch");
+  if (a.kalman_init) e->kalman_first = false;
+  OlaArgs o{};
+  o.g = a.g;
+  o.blocks = e->d_blocks;
+  o.dst = ddst;
+  o.pitch = pitch;
+  o.fmt = fmt;
+  o.chroma_norm = e->cnorm;
+  o.inv_norm = e->inv_norm;
+  o.max_pix = e->max_pix;
+  ce = launch_ola(o, e->stream);
+  cudaEventRecord(e->ev[3], e->stream);
+  e->proc_timed = true;
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "the overlap-add launch");
+  return F3D_OK;
+}
+
+struct Lock {
+  std::lock_guard<std::mutex> g;
+  explicit Lock(f3d_engine* e) : g(e->mtx) { cudaSetDevice(e->device); }
+};
+
+}  // namespace
+
+extern "C" {
+
+void f3d_default_params(f3d_script_params* sp) {
+  // ScriptParams defaults, src/params.h:8-27, with the plugin's dependent
+  // defaults applied to them (src/fft3dcl.cpp:182-194).
+  sp->sigma = 2.0f;
+  sp->beta = 1.0f;
+  sp->bw = sp->bh = 32;
+  sp->bt = 3;
+  sp->sharpen = 0.0f;
+  sp->plane = 0;
+  sp->mode = 1;
+  sp->bordersize = 1;
+  sp->precision = 0;
+  sp->degrid = 1.0f;
+  sp->scutoff = 0.3f;
+  sp->svr = 1.0f;
+  sp->smin = 4.0f;
+  sp->smax = 20.0f;
+  sp->kratio = 2.0f;
+  sp->ow = sp->oh = 16;
+  sp->wintype = 0;
+  sp->interlaced = 0;
+  sp->sigma2 = sp->sigma3 = sp->sigma4 = 2.0f;
+  sp->oldfft = -1;
+}
+
+int f3d_validate_params(const f3d_script_params* sp, int width, int height, int bits,
+                        f3d_internal_params* out) {
+  if (!sp || !out) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  std::string err;
+  if (!validate_params(*sp, width, height, bits, *out, &err)) return fail_thread(F3D_E_PARAM, err);
+  return F3D_OK;
+}
+
+const char* f3d_last_error(void) { return t_last_error.c_str(); }
+
+int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
+                      const f3d_options* opts, f3d_engine** out) {
+  if (!sp || !geom || !out) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  *out = nullptr;
+  const f3d_plane_geom& g = *geom;
+  if (g.width <= 0 || g.height <= 0)
+    return fail_thread(F3D_E_PARAM, "FFT3DCL: plane size must be positive");
+  if (g.sample_type == 1 ? g.bits != 32 : (g.bits < 8 || g.bits > 16))
+    return fail_thread(F3D_E_PARAM, "FFT3DCL: integer bit depths 8-16 and 32-bit float only");
+  f3d_internal_params ip;
+  std::string err;
+  if (!validate_params(*sp, g.width, g.height, g.bits, ip, &err)) return fail_thread(F3D_E_PARAM, err);
+  const int form = opts ? opts->form : F3D_FORM_EXACT;
+  const int device = opts ? opts->device : 0;
+  if (!form_supported(form, ip.bw, ip.bh))
+    return fail_thread(F3D_E_UNSUPPORTED,
+                       "FFT3DCL: block size " + std::to_string(ip.bw) + "x" + std::to_string(ip.bh) +
+                           " is not supported by this GPU form (powers of two 4..64)");
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return fail_thread(F3D_E_CUDA, std::string("FFT3DCL: no CUDA device available: ") +
+                                       (ce != cudaSuccess ? cudaGetErrorString(ce) : "none found"));
+  }
+  if (device < 0 || device >= ndev) return fail_thread(F3D_E_PARAM, "FFT3DCL: device ordinal out of range");
+  ce = cudaSetDevice(device);
+  if (ce != cudaSuccess) return fail_thread(F3D_E_CUDA, std::string("FFT3DCL: cudaSetDevice: ") + cudaGetErrorString(ce));
+
+  auto* e = new f3d_engine();
+  ++g_live;
+  e->ip = ip;
+  e->geom = g;
+  e->grid = make_grid(ip);
+  e->device = device;
+  e->form = form;
+  e->fbw = ip.bw / 2 + 1;
+  e->ps = e->fbw * ip.bh;
+  e->spec_bytes = sizeof(float2) * (size_t)e->grid.nb * e->ps;
+  if (g.sample_type == 1) {
+    e->fmt = FMT_F32;
+    e->bps = 4;
+  } else if (g.bits <= 8) {
+    e->fmt = FMT_U8;
+    e->bps = 1;
+  } else {
+    e->fmt = FMT_U16;
+    e->bps = 2;
+    // Conversion constants of src/cpu/reference.cpp:97-98 and :126-127.
+    e->norm = (float)(1u << (16 - g.bits)) / 65535.0f;
+    e->inv_norm = 1.0f / (float)(1u << (16 - g.bits));
+    e->max_pix = (float)((1u << g.bits) - 1);
+  }
+  e->cnorm = chroma_norm(ip, g);
+  e->tw_row = twiddles(ip.bw);
+  e->tw_col = twiddles(ip.bh);
+  if (ip.mode == 0) {
+    e->win_ana = window_mode0(ip.bw, ip.bh);
+  } else {
+    windows_mode1(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, e->win_ana, e->syn_a, e->syn_b);
+  }
+  if (ip.use_pattern)
+    e->pattern = sigma_pattern(ip.bw, ip.bh, ip.bt, ip.sigma * 255.0f, ip.sigma2, ip.sigma3, ip.sigma4);
+  if (ip.sharpen_on) e->sharpen = sharpen_lut(ip.bw, ip.bh, ip.sharpen, ip.svr, ip.scutoff);
+  if (ip.degrid_on) e->gs = degrid_sample(ip.bw, ip.bh, ip.degrid, e->win_ana);
+
+  auto finish_fail = [&](int code) {
+    std::string m = e->err;
+    f3d_engine_destroy(e);
+    return fail_thread(code, m);
+  };
+  if (opts && opts->stream) {
+    e->stream = static_cast<cudaStream_t>(opts->stream);
+  } else {
+    ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) return finish_fail(e->cuda_fail(ce, "stream creation"));
+    e->own_stream = true;
+  }
+  for (auto& ev : e->ev) {
+    ce = cudaEventCreate(&ev);
+    if (ce != cudaSuccess) return finish_fail(e->cuda_fail(ce, "event creation"));
+  }
+  const size_t bwbh = (size_t)ip.bw * ip.bh;
+  const size_t plane_bytes = (size_t)g.width * g.height * 4;
+  auto up = [&](float** d, const std::vector<float>& h) -> cudaError_t {
+    if (h.empty()) return cudaSuccess;
+    cudaError_t x = e->alloc(d, h.size() * sizeof(float));
+    if (x != cudaSuccess) return x;
+    return cudaMemcpy(*d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice);
+  };
+  if ((ce = up(&e->d_win_ana, e->win_ana)) != cudaSuccess ||
+      (ce = up(&e->d_syn_a, e->syn_a)) != cudaSuccess ||
+      (ce = up(&e->d_syn_b, e->syn_b)) != cudaSuccess ||
+      (ce = up(&e->d_pattern, e->pattern)) != cudaSuccess ||
+      (ce = up(&e->d_sharpen, e->sharpen)) != cudaSuccess ||
+      (ce = up(reinterpret_cast<float**>(&e->d_gs), e->gs)) != cudaSuccess)
+    return finish_fail(e->cuda_fail(ce, "table upload"));
+  if ((ce = e->alloc(&e->d_in, plane_bytes)) != cudaSuccess ||
+      (ce = e->alloc(&e->d_out, plane_bytes)) != cudaSuccess ||
+      (ce = e->alloc(&e->d_blocks, sizeof(float) * bwbh * e->grid.nb)) != cudaSuccess)
+    return finish_fail(e->cuda_fail(ce, "buffer allocation"));
+  if (ip.bm == 0) {
+    const size_t nbin = (size_t)e->grid.nb * e->ps;
+    if ((ce = e->alloc(&e->d_klast, sizeof(float2) * nbin)) != cudaSuccess ||
+        (ce = e->alloc(&e->d_kcov, sizeof(float) * nbin)) != cudaSuccess ||
+        (ce = e->alloc(&e->d_kproc, sizeof(float) * nbin)) != cudaSuccess)
+      return finish_fail(e->cuda_fail(ce, "Kalman state allocation"));
+  }
+  *out = e;
+  return F3D_OK;
+}
+
+void f3d_engine_destroy(f3d_engine* e) {
+  if (!e) return;
+  {
+    Lock l(e);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    for (auto& kv : e->cache) e->release(kv.second, e->spec_bytes);
+    e->cache.clear();
+    for (float2*& m : e->pool) e->release(m, e->spec_bytes);
+    e->pool.clear();
+    e->release(e->d_win_ana, e->win_ana.size() * sizeof(float));
+    e->release(e->d_syn_a, e->syn_a.size() * sizeof(float));
+    e->release(e->d_syn_b, e->syn_b.size() * sizeof(float));
+    e->release(e->d_pattern, e->pattern.size() * sizeof(float));
+    e->release(e->d_sharpen, e->sharpen.size() * sizeof(float));
+    e->release(e->d_gs, e->gs.size() * sizeof(float));
+    const size_t plane_bytes = (size_t)e->geom.width * e->geom.height * 4;
+    e->release(e->d_in, plane_bytes);
+    e->release(e->d_out, plane_bytes);
+    e->release(e->d_blocks, sizeof(float) * (size_t)e->ip.bw * e->ip.bh * e->grid.nb);
+    const size_t nbin = (size_t)e->grid.nb * e->ps;
+    e->release(e->d_klast, sizeof(float2) * nbin);
+    e->release(e->d_kcov, sizeof(float) * nbin);
+    e->release(e->d_kproc, sizeof(float) * nbin);
+    for (auto& ev : e->ev)
+      if (ev) cudaEventDestroy(ev);
+    if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
+  }
+  --g_live;
+  delete e;
+}
+
+const char* f3d_engine_error(const f3d_engine* e) { return e ? e->err.c_str() : ""; }
+
+int f3d_engine_get_info(f3d_engine* e, f3d_engine_info* info) {
+  if (!e || !info) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  info->nblocks = e->grid.nb;
+  info->fbw = e->fbw;
+  info->ncols = e->grid.ncols;
+  info->nrows = e->grid.nrows;
+  info->bytes_per_sample = e->bps;
+  info->raw_path = e->geom.sample_type != 1;
+  info->spectrum_bytes = e->spec_bytes;
+  info->device_bytes = e->bytes;
+  info->cached_frames = (int)e->cache.size();
+  info->chroma_norm = e->cnorm;
+  return F3D_OK;
+}
+
+int f3d_engine_get_table(f3d_engine* e, int which, float* dst) {
+  if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine");
+  Lock l(e);
+  const std::vector<float>* t = nullptr;
+  std::vector<float> tmp;
+  switch (which) {
+  case F3D_TAB_WIN_ANA: t = &e->win_ana; break;
+  case F3D_TAB_WIN_SYN_A: t = &e->syn_a; break;
+  case F3D_TAB_WIN_SYN_B: t = &e->syn_b; break;
+  case F3D_TAB_PATTERN: t = &e->pattern; break;
+  case F3D_TAB_SHARPEN: t = &e->sharpen; break;
+  case F3D_TAB_GS_RE:
+  case F3D_TAB_GS_IM:
+    for (size_t i = (which == F3D_TAB_GS_IM); i < e->gs.size(); i += 2) tmp.push_back(e->gs[i]);
+    t = &tmp;
+    break;
+  case F3D_TAB_TWIDDLE_ROW: t = &e->tw_row; break;
+  case F3D_TAB_TWIDDLE_COL: t = &e->tw_col; break;
+  default: return e->fail(F3D_E_PARAM, "FFT3DCL: unknown table");
+  }
+  if (dst && !t->empty()) std::memcpy(dst, t->data(), t->size() * sizeof(float));
+  return (int)t->size();
+}
+
+int f3d_forward(f3d_engine* e, int fn, const float* plane) {
+  if (!e || !plane) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  const size_t n = (size_t)e->geom.width * e->geom.height * sizeof(float);
+  cudaError_t ce = cudaMemcpyAsync(e->d_in, plane, n, cudaMemcpyHostToDevice, e->stream);
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "the plane upload");
+  return run_forward(e, fn, e->d_in, (long long)e->geom.width * 4, FMT_F32);
+}
+
+int f3d_forward_raw(f3d_engine* e, int fn, const void* raw, size_t bytes) {
+  if (!e || !raw) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  const size_t row = (size_t)e->geom.width * e->bps;
+  if (bytes != row * e->geom.height) return e->fail(F3D_E_PARAM, "FFT3DCL: raw plane size mismatch");
+  cudaError_t ce = cudaMemcpyAsync(e->d_in, raw, bytes, cudaMemcpyHostToDevice, e->stream);
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "the raw plane upload");
+  return run_forward(e, fn, e->d_in, (long long)row, e->fmt);
+}
+
+int f3d_forward_device(f3d_engine* e, int fn, const void* dev_plane, size_t pitch) {
+  if (!e || !dev_plane) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  if (pitch < (size_t)e->geom.width * e->bps) return e->fail(F3D_E_PARAM, "FFT3DCL: pitch too small");
+  return run_forward(e, fn, static_cast<const uint8_t*>(dev_plane), (long long)pitch, e->fmt);
+}
+
+int f3d_get_spectra(f3d_engine* e, int fn, float* dst) {
+  if (!e || !dst) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  const float2* s = spectra_slot(e, fn, false);
+  if (!s) return e->fail(F3D_E_STATE, "FFT3DCL: frame " + std::to_string(fn) + " is not cached");
+  cudaError_t ce = cudaMemcpyAsync(dst, s, e->spec_bytes, cudaMemcpyDeviceToHost, e->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "spectra readback");
+  return F3D_OK;
+}
+
+int f3d_has(f3d_engine* e, int fn) {
+  if (!e) return 0;
+  Lock l(e);
+  return e->cache.count(fn) ? 1 : 0;
+}
+
+int f3d_raw_path(f3d_engine* e) { return e && e->geom.sample_type != 1 ? 1 : 0; }
+int f3d_bytes_per_sample(f3d_engine* e) { return e ? e->bps : 0; }
+
+int f3d_upload_degrid_sample(f3d_engine* e) {
+  if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine");
+  Lock l(e);
+  if (e->ip.degrid_on) e->degrid_active = true;
+  return F3D_OK;
+}
+
+int f3d_process(f3d_engine* e, const int* window, int n, float* out) {
+  if (!e || !out) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  const size_t row = (size_t)e->geom.width * 4;
+  int rc = run_process(e, window, n, e->d_out, (long long)row, FMT_F32);
+  if (rc != F3D_OK) return rc;
+  cudaError_t ce = cudaMemcpyAsync(out, e->d_out, row * e->geom.height, cudaMemcpyDeviceToHost, e->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "readback");
+  return F3D_OK;
+}
+
+int f3d_process_raw(f3d_engine* e, const int* window, int n, void* dst, size_t bytes) {
+  if (!e || !dst) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  const size_t row = (size_t)e->geom.width * e->bps;
+  if (bytes != row * e->geom.height) return e->fail(F3D_E_PARAM, "FFT3DCL: raw plane size mismatch");
+  int rc = run_process(e, window, n, e->d_out, (long long)row, e->fmt);
+  if (rc != F3D_OK) return rc;
+  cudaError_t ce = cudaMemcpyAsync(dst, e->d_out, bytes, cudaMemcpyDeviceToHost, e->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "readback");
+  return F3D_OK;
+}
+
+int f3d_process_device(f3d_engine* e, const int* window, int n, void* dev_dst, size_t pitch) {
+  if (!e || !dev_dst) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  if (pitch < (size_t)e->geom.width * e->bps) return e->fail(F3D_E_PARAM, "FFT3DCL: pitch too small");
+  return run_process(e, window, n, static_cast<uint8_t*>(dev_dst), (long long)pitch, e->fmt);
+}
+
+int f3d_prune(f3d_engine* e, int lo, int hi) {
+  if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine");
+  Lock l(e);
+  for (auto it = e->cache.begin(); it != e->cache.end();) {
+    const bool keep = (lo < 0 || it->first >= lo) && (hi < 0 || it->first <= hi);
+    if (keep) {
+      ++it;
+    } else {
+      retire(e, it->second);
+      it = e->cache.erase(it);
+    }
+  }
+  return F3D_OK;
+}
+
+int f3d_synchronize(f3d_engine* e) {
+  if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine");
+  Lock l(e);
+  cudaError_t ce = cudaStreamSynchronize(e->stream);
+  if (ce != cudaSuccess) return e->cuda_fail(ce, "synchronize");
+  return F3D_OK;
+}
+
+int f3d_last_kernel_ms(f3d_engine* e, float* ms) {
+  if (!e || !ms) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  Lock l(e);
+  ms[0] = ms[1] = ms[2] = -1.0f;
+  if (e->fwd_timed) cudaEventElapsedTime(&ms[0], e->ev[0], e->ev[1]);
+  if (e->proc_timed) {
+    cudaEventElapsedTime(&ms[1], e->ev[2], e->ev[4]);
+    cudaEventElapsedTime(&ms[2], e->ev[4], e->ev[3]);
+  }
+  cudaGetLastError();
+  return F3D_OK;
+}
+
+int f3d_live_instances(void) { return g_live.load(); }
+size_t f3d_live_bytes(void) { return g_bytes.load(); }
+uint64_t f3d_kernel_launches(void) { return launch_count(); }
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// f3d_kernels.hpp -- launch interface between the engine (host C++) and the
+// CUDA kernels. Plain structs passed by value as __grid_constant__ kernel
+// parameters, so tables that every thread reads with compile-time indices
+// (the FFT twiddles) sit in the constant bank.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace f3d {
+
+// Plane geometry and block grid as the kernels see it.
+struct Geo {
+  int W, H;          // plane size in samples
+  int bw, bh, fbw;   // block size, kept spectrum columns (bw/2+1)
+  int nb;            // blocks in the plane
+  int mode;          // 0: two offset grids, 1: overlapped grid
+  int ncols, nrows;  // mode 1: blocks per row / rows; mode 0: nx, ny per grid
+  int xoff, xstep, yoff, ystep;
+};
+
+// Sample formats of the raw planes.
+enum Fmt : int { FMT_F32 = 0, FMT_U8 = 8, FMT_U16 = 16 };
+
+// FFT twiddles of the reference plans (double -> float), N/2 entries each,
+// for the row (bw) and column (bh) lengths.
+struct Twiddles {
+  float2 row[32];
+  float2 col[32];
+};
+
+struct FwdArgs {
+  Geo g;
+  Twiddles tw;
+  const uint8_t* src;  // plane in device memory
+  long long pitch;     // bytes between rows
+  int fmt;
+  float norm;          // 16-bit: 2^(16-bits)/65535
+  float chroma_norm;   // subtracted before windowing (mode-1 chroma)
+  const float* win;    // analysis window, bw*bh
+  float2* spec;        // out: nb x bh x fbw half spectra
+};
+
+struct InvArgs {
+  Geo g;
+  Twiddles tw;
+  const float2* s[4];  // window spectra in temporal order
+  int cur;             // index of the current frame in s
+  int bm;              // temporal mode -1..4
+  int dg, pat, shp;    // degrid, sigma pattern, sharpen on
+  int kalman_init;     // bt=0: first frame, state starts from s[0]
+  const float2* gs;    // degrid sample, bh x fbw
+  const float* pattern;
+  const float* sharpen;
+  float2* klast;       // Kalman state, nb x bh x fbw
+  float* kcov;
+  float* kproc;
+  const float* win_a;  // synthesis window of even-parity blocks (mode 0: analysis window)
+  const float* win_b;  // synthesis window of odd-parity blocks
+  float* blocks;       // out: nb x bh x bw windowed blocks
+  float sigma_x, sigma_y, beta_x, beta, ssmin, ssmax, kalman_cn, kr2;
+};
+
+struct OlaArgs {
+  Geo g;
+  const float* blocks;
+  uint8_t* dst;
+  long long pitch;
+  int fmt;
+  float chroma_norm, inv_norm, max_pix;
+};
+
+// Kernel launches; each returns the launch error. `form` is F3D_FORM_*.
+cudaError_t launch_forward(int form, const FwdArgs& a, cudaStream_t st);
+cudaError_t launch_filter_inverse(int form, const InvArgs& a, cudaStream_t st);
+cudaError_t launch_ola(const OlaArgs& a, cudaStream_t st);
+// True when kernels of this form exist for this block size.
+bool form_supported(int form, int bw, int bh);
+
+// Exact-form launchers, one translation unit per block width.
+#define F3D_DECLARE_EXACT(BW)                                                        \
+  cudaError_t launch_forward_exact_bw##BW(const FwdArgs& a, cudaStream_t st);        \
+  cudaError_t launch_inverse_exact_bw##BW(const InvArgs& a, cudaStream_t st);
+F3D_DECLARE_EXACT(4)
+F3D_DECLARE_EXACT(8)
+F3D_DECLARE_EXACT(16)
+F3D_DECLARE_EXACT(32)
+F3D_DECLARE_EXACT(64)
+#undef F3D_DECLARE_EXACT
+
+// Counts one kernel launch made by this library (all engines, all threads).
+void count_launch();
+
+} // namespace f3d

@@ -1,0 +1,189 @@
+/*
+ * fft3d_gb300.h -- C ABI of the GB300 FFT3D block-FFT denoise engine.
+ *
+ * One engine handles one plane of one filter instance, the unit the reference
+ * backend works in (class GpuRef, src/cl/gpu.h:16-88 of HumbleUser33/FFT3dCL).
+ * Each entry point below names the reference member it replaces. Plain C types
+ * only; a cudaStream_t is passed as void*.
+ *
+ * Per frame a host does what the reference plugin does (src/fft3dcl.cpp:388-468):
+ *   for each frame of the temporal window: if (!f3d_has(e, fn)) f3d_forward_raw(e, fn, ...);
+ *   f3d_process_raw(e, window, n, dst, bytes);
+ *   f3d_prune(e, lo, hi);
+ *
+ * Errors: every call returns F3D_OK (0) or a negative F3D_E_* code. The
+ * message is kept per engine (f3d_engine_error) and, for calls without an
+ * engine, per thread (f3d_last_error). There is no CPU fallback: when the
+ * CUDA path cannot run, the call fails.
+ *
+ * Threading: all calls on one engine are serialised by the engine's own
+ * mutex (the reference serialises one instance with a mutex,
+ * src/fft3dcl.cpp:365-368). Different engines may be driven from different
+ * threads.
+ */
+#ifndef FFT3D_GB300_H
+#define FFT3D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define F3D_ABI_VERSION 1
+
+enum {
+  F3D_OK = 0,
+  F3D_E_PARAM = -1,     /* invalid parameters or arguments                */
+  F3D_E_CUDA = -2,      /* a CUDA call failed (message has the reason)    */
+  F3D_E_NOMEM = -3,     /* device allocation failed                       */
+  F3D_E_STATE = -4,     /* call out of order (missing spectra, ...)       */
+  F3D_E_UNSUPPORTED = -5 /* feature not available on this path           */
+};
+
+/* Script-level parameters: names, types and defaults of ScriptParams,
+ * src/params.h:8-27. f3d_default_params fills the defaults. */
+typedef struct {
+  float sigma, beta;
+  int bw, bh, bt;
+  float sharpen;
+  int plane, mode, bordersize, precision;
+  float degrid, scutoff, svr, smin, smax, kratio;
+  int ow, oh, wintype, interlaced;
+  float sigma2, sigma3, sigma4;
+  int oldfft;
+} f3d_script_params;
+
+/* Validated parameters: InternalParams, src/params.h:30-59. */
+typedef struct {
+  float sigma, beta;
+  int bw, bh, bm, bt;
+  float sharpen;
+  int sharpen_on, mode, bordersize, precision;
+  float degrid;
+  int degrid_on;
+  float scutoff, svr, smin, smax, kratio;
+  int ow, oh, wintype, interlaced;
+  float sigma2, sigma3, sigma4;
+  int use_pattern, current, nx, ny, totw, toth, oldfft;
+  float wiener_s, beta_x, kalman_cn, ssmin, ssmax;
+} f3d_internal_params;
+
+/* Plane geometry: PlaneGeom, src/cpu/reference.h:17-22. */
+typedef struct {
+  int width, height;
+  int bits;        /* 8..16 for integer samples, 32 for float */
+  int sample_type; /* 0 integer, 1 float                       */
+  int chroma;      /* YUV chroma plane (mode-1 centering)      */
+} f3d_plane_geom;
+
+/* Arithmetic form of the block transforms. */
+enum {
+  F3D_FORM_EXACT = 0, /* radix-2 DIT in the reference's operation order, no
+                         fused multiply-add: same bits as the CPU backend   */
+  F3D_FORM_FAST = 1,  /* packed real FFTs with FMA, fp32                     */
+  F3D_FORM_TC = 2     /* DFT-matrix contraction on the tensor cores          */
+};
+
+typedef struct {
+  int device;   /* CUDA device ordinal                                   */
+  int form;     /* F3D_FORM_*                                            */
+  void* stream; /* cudaStream_t to run on, NULL: the engine makes one    */
+} f3d_options;
+
+typedef struct {
+  int nblocks, fbw, ncols, nrows;
+  int bytes_per_sample;
+  int raw_path;
+  size_t spectrum_bytes; /* one frame's half spectra in HBM */
+  size_t device_bytes;   /* all device memory held by the engine */
+  int cached_frames;
+  float chroma_norm;
+} f3d_engine_info;
+
+typedef struct f3d_engine f3d_engine;
+
+/* Plugin argument defaults (src/fft3dcl.cpp:171-195) for bw/bh/mode/sigma
+ * as given: degrid = mode==1 ? 1 : 0, ow/oh = bw/2, bh/2, sigma2..4 = sigma. */
+void f3d_default_params(f3d_script_params* sp);
+
+/* validateParams, src/params.h:76-148 (roundPow2Clamp :62-72). */
+int f3d_validate_params(const f3d_script_params* sp, int width, int height, int bits,
+                        f3d_internal_params* out);
+
+/* Thread-local message of the last failing call made without an engine. */
+const char* f3d_last_error(void);
+
+/* GpuRef::GpuRef (src/cl/gpu.cpp:59-245): validates, builds the block grid
+ * and all tables (windows, sigma pattern, sharpen LUT, degrid sample) and
+ * allocates the device buffers. */
+int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
+                      const f3d_options* opts, f3d_engine** out);
+/* GpuRef::~GpuRef (src/cl/gpu.cpp:247-270). */
+void f3d_engine_destroy(f3d_engine* e);
+/* GpuRef::error (src/cl/gpu.h:23). */
+const char* f3d_engine_error(const f3d_engine* e);
+int f3d_engine_get_info(f3d_engine* e, f3d_engine_info* info);
+/* Host copy of an engine table (F3D_TAB_*); returns the float count. */
+int f3d_engine_get_table(f3d_engine* e, int which, float* dst);
+
+enum {
+  F3D_TAB_WIN_ANA = 0, F3D_TAB_WIN_SYN_A, F3D_TAB_WIN_SYN_B, F3D_TAB_PATTERN,
+  F3D_TAB_SHARPEN, F3D_TAB_GS_RE, F3D_TAB_GS_IM, F3D_TAB_TWIDDLE_ROW, F3D_TAB_TWIDDLE_COL
+};
+
+/* GpuRef::forward (src/cl/gpu.cpp:326-347): forward transform of a host float
+ * plane (width*height floats, packed), cached as frame fn. */
+int f3d_forward(f3d_engine* e, int fn, const float* plane);
+/* GpuRef::forwardRaw (src/cl/gpu.cpp:349-372): same from the plane's native
+ * samples, `bytes` = width*height*bytes_per_sample, packed rows. */
+int f3d_forward_raw(f3d_engine* e, int fn, const void* raw, size_t bytes);
+/* Same from a plane already in device memory, rows `pitch` bytes apart. */
+int f3d_forward_device(f3d_engine* e, int fn, const void* dev_plane, size_t pitch);
+/* Host copy of the cached half spectra of frame fn: nblocks x bh x fbw
+ * complex values, interleaved re, im (the device layout). For tests and
+ * tooling; the reference keeps them device-only (src/cl/gpu.h:79). */
+int f3d_get_spectra(f3d_engine* e, int fn, float* dst);
+/* GpuRef::has (src/cl/gpu.h:35). */
+int f3d_has(f3d_engine* e, int fn);
+/* GpuRef::rawPath / bytesPerSample (src/cl/gpu.h:37-38). */
+int f3d_raw_path(f3d_engine* e);
+int f3d_bytes_per_sample(f3d_engine* e);
+/* GpuRef::uploadDegridSample (src/cl/gpu.cpp:374-387). The engine builds the
+ * degrid sample itself; this only makes it active (it is also made active by
+ * the first process call when degrid is on). */
+int f3d_upload_degrid_sample(f3d_engine* e);
+
+/* GpuRef::process (src/cl/gpu.cpp:460-482): filter + inverse + overlap-add
+ * of the window frames (frame numbers in temporal order, bt of them for
+ * bt >= 2, else one); out receives width*height floats. */
+int f3d_process(f3d_engine* e, const int* window, int n, float* out);
+/* GpuRef::processRaw (src/cl/gpu.cpp:484-505): same, packed to the native
+ * sample format into dst (`bytes` = width*height*bytes_per_sample). */
+int f3d_process_raw(f3d_engine* e, const int* window, int n, void* dst, size_t bytes);
+/* Same into device memory, rows `pitch` bytes apart; returns once queued. */
+int f3d_process_device(f3d_engine* e, const int* window, int n, void* dev_dst, size_t pitch);
+
+/* GpuRef::pruneCache (src/cl/gpu.cpp:507-517): drop cached spectra outside
+ * [lo, hi]; a negative bound is disabled. */
+int f3d_prune(f3d_engine* e, int lo, int hi);
+
+/* Wait for all queued work of the engine. */
+int f3d_synchronize(f3d_engine* e);
+/* Device time of the kernels of the last forward / process calls in ms:
+ * ms[0] forward transform, ms[1] filter + inverse, ms[2] overlap-add + pack
+ * (CUDA events on the engine stream; valid after f3d_synchronize). */
+int f3d_last_kernel_ms(f3d_engine* e, float* ms);
+
+/* GpuRef::liveInstances / liveBytes (src/cl/gpu.cpp:44-57). */
+int f3d_live_instances(void);
+size_t f3d_live_bytes(void);
+
+/* Number of kernel launches made by this library since load (all engines). */
+uint64_t f3d_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
