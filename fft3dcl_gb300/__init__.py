@@ -89,6 +89,7 @@ class EngineInfo(C.Structure):
 EXPORTS = (
     "f3d_default_params", "f3d_validate_params", "f3d_last_error", "f3d_engine_create",
     "f3d_engine_destroy", "f3d_engine_error", "f3d_engine_get_info", "f3d_engine_get_table",
+    "f3d_compute_table",
     "f3d_forward", "f3d_forward_raw", "f3d_forward_device", "f3d_get_spectra", "f3d_has", "f3d_raw_path",
     "f3d_bytes_per_sample", "f3d_upload_degrid_sample", "f3d_process", "f3d_process_raw",
     "f3d_process_device", "f3d_prune", "f3d_synchronize", "f3d_last_kernel_ms",
@@ -119,6 +120,7 @@ def lib():
         L.f3d_engine_error.restype = C.c_char_p
         L.f3d_engine_get_info.argtypes = [vp, P(EngineInfo)]
         L.f3d_engine_get_table.argtypes = [vp, i, vp]
+        L.f3d_compute_table.argtypes = [P(ScriptParams), P(PlaneGeom), i, vp]
         L.f3d_forward.argtypes = [vp, i, vp]
         L.f3d_forward_raw.argtypes = [vp, i, vp, sz]
         L.f3d_forward_device.argtypes = [vp, i, vp, sz]
@@ -187,6 +189,20 @@ def validate(width: int, height: int, bits: int, **params) -> InternalParams:
                                  C.byref(ip)) != F3D_OK:
         raise ValueError(lib().f3d_last_error().decode())
     return ip
+
+
+def compute_table(which: int, width: int, height: int, bits: int = 8, sample_type: int = 0,
+                  chroma: bool = False, **params) -> np.ndarray:
+    """A plane table (TAB_*) computed on the host, without a device."""
+    sp = script_params(**params)
+    g = PlaneGeom(width, height, bits, sample_type, int(chroma))
+    n = lib().f3d_compute_table(C.byref(sp), C.byref(g), which, None)
+    if n < 0:
+        raise ValueError(lib().f3d_last_error().decode())
+    out = np.zeros(n, np.float32)
+    if n:
+        lib().f3d_compute_table(C.byref(sp), C.byref(g), which, out.ctypes.data_as(C.c_void_p))
+    return out
 
 
 def live_instances() -> int:

@@ -36,6 +36,9 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # Exact form: no fused multiply-add, IEEE division and square root, no
 # flush-to-zero -- every fp32 operation rounds like the reference CPU code.
 NVCC_EXACT = ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
+# Host code builds the tables the kernels read; GCC fuses multiply-adds in
+# C++ by default on aarch64, which would change their last bits there.
+HOST_CXX = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-ffp-contract=off"]
 
 
 def _units():
@@ -59,7 +62,7 @@ def _units():
         if not os.path.exists(src):
             continue
         obj = os.path.join(BUILD, name.replace(".cpp", ".o"))
-        units.append((obj, ["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", "-I", INC, "-I", CSRC,
+        units.append((obj, ["g++"] + HOST_CXX + ["-I", INC, "-I", CSRC,
                             "-I", os.path.join(CUDA, "include"), "-c", src, "-o", obj], [src] + headers))
     return units
 
@@ -120,7 +123,7 @@ def build(verbose: bool = False) -> str:
     if vsinc and os.path.exists(psrc):
         pobj = os.path.join(BUILD, "f3d_plugin.o")
         if _stale(pobj, [psrc] + glob.glob(os.path.join(CSRC, "*.hpp"))):
-            _run(["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", "-I", INC, "-I", CSRC, "-I", vsinc,
+            _run(["g++"] + HOST_CXX + ["-I", INC, "-I", CSRC, "-I", vsinc,
                   "-c", psrc, "-o", pobj])
         if _stale(PLUGIN, [pobj] + objs):
             _run([NVCC] + ARCH + ["-shared", "-o", PLUGIN, pobj] + objs + ["-lpthread"])

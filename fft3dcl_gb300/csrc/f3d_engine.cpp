@@ -343,17 +343,17 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
     e->max_pix = (float)((1u << g.bits) - 1);
   }
   e->cnorm = chroma_norm(ip, g);
-  e->tw_row = twiddles(ip.bw);
-  e->tw_col = twiddles(ip.bh);
-  if (ip.mode == 0) {
-    e->win_ana = window_mode0(ip.bw, ip.bh);
-  } else {
-    windows_mode1(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, e->win_ana, e->syn_a, e->syn_b);
+  {
+    PlaneTables t = build_tables(ip);
+    e->tw_row = std::move(t.tw_row);
+    e->tw_col = std::move(t.tw_col);
+    e->win_ana = std::move(t.win_ana);
+    e->syn_a = std::move(t.syn_a);
+    e->syn_b = std::move(t.syn_b);
+    e->pattern = std::move(t.pattern);
+    e->sharpen = std::move(t.sharpen);
+    e->gs = std::move(t.gs);
   }
-  if (ip.use_pattern)
-    e->pattern = sigma_pattern(ip.bw, ip.bh, ip.bt, ip.sigma * 255.0f, ip.sigma2, ip.sigma3, ip.sigma4);
-  if (ip.sharpen_on) e->sharpen = sharpen_lut(ip.bw, ip.bh, ip.sharpen, ip.svr, ip.scutoff);
-  if (ip.degrid_on) e->gs = degrid_sample(ip.bw, ip.bh, ip.degrid, e->win_ana);
 
   auto finish_fail = [&](int code) {
     std::string m = e->err;
@@ -452,26 +452,25 @@ int f3d_engine_get_info(f3d_engine* e, f3d_engine_info* info) {
 
 int f3d_engine_get_table(f3d_engine* e, int which, float* dst) {
   if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine");
+  if (which < F3D_TAB_WIN_ANA || which > F3D_TAB_TWIDDLE_COL)
+    return e->fail(F3D_E_PARAM, "FFT3DCL: unknown table");
   Lock l(e);
-  const std::vector<float>* t = nullptr;
-  std::vector<float> tmp;
-  switch (which) {
-  case F3D_TAB_WIN_ANA: t = &e->win_ana; break;
-  case F3D_TAB_WIN_SYN_A: t = &e->syn_a; break;
-  case F3D_TAB_WIN_SYN_B: t = &e->syn_b; break;
-  case F3D_TAB_PATTERN: t = &e->pattern; break;
-  case F3D_TAB_SHARPEN: t = &e->sharpen; break;
-  case F3D_TAB_GS_RE:
-  case F3D_TAB_GS_IM:
-    for (size_t i = (which == F3D_TAB_GS_IM); i < e->gs.size(); i += 2) tmp.push_back(e->gs[i]);
-    t = &tmp;
-    break;
-  case F3D_TAB_TWIDDLE_ROW: t = &e->tw_row; break;
-  case F3D_TAB_TWIDDLE_COL: t = &e->tw_col; break;
-  default: return e->fail(F3D_E_PARAM, "FFT3DCL: unknown table");
-  }
-  if (dst && !t->empty()) std::memcpy(dst, t->data(), t->size() * sizeof(float));
-  return (int)t->size();
+  PlaneTables t{e->win_ana, e->syn_a, e->syn_b, e->pattern, e->sharpen, e->gs, e->tw_row, e->tw_col};
+  const std::vector<float> v = table_of(t, which);
+  if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(float));
+  return (int)v.size();
+}
+
+int f3d_compute_table(const f3d_script_params* sp, const f3d_plane_geom* geom, int which, float* dst) {
+  if (!sp || !geom) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  if (which < F3D_TAB_WIN_ANA || which > F3D_TAB_TWIDDLE_COL)
+    return fail_thread(F3D_E_PARAM, "FFT3DCL: unknown table");
+  f3d_internal_params ip;
+  std::string err;
+  if (!validate_params(*sp, geom->width, geom->height, geom->bits, ip, &err)) return fail_thread(F3D_E_PARAM, err);
+  const std::vector<float> v = table_of(build_tables(ip), which);
+  if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(float));
+  return (int)v.size();
 }
 
 int f3d_forward(f3d_engine* e, int fn, const float* plane) {

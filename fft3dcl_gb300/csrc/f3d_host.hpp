@@ -360,6 +360,49 @@ inline std::vector<float> degrid_sample(int bw, int bh, float degrid, const std:
   return gs;
 }
 
+// All host tables of one plane (the PlaneRef constructor,
+// src/cpu/reference.cpp:19-61, and buildDegridSample :172-198). Tables that
+// are off stay empty; twiddles and the degrid sample are interleaved re, im.
+struct PlaneTables {
+  std::vector<float> win_ana, syn_a, syn_b, pattern, sharpen, gs, tw_row, tw_col;
+};
+
+inline PlaneTables build_tables(const f3d_internal_params& ip) {
+  PlaneTables t;
+  t.tw_row = twiddles(ip.bw);
+  t.tw_col = twiddles(ip.bh);
+  if (ip.mode == 0)
+    t.win_ana = window_mode0(ip.bw, ip.bh);
+  else
+    windows_mode1(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, t.win_ana, t.syn_a, t.syn_b);
+  if (ip.use_pattern)
+    t.pattern = sigma_pattern(ip.bw, ip.bh, ip.bt, ip.sigma * 255.0f, ip.sigma2, ip.sigma3, ip.sigma4);
+  if (ip.sharpen_on) t.sharpen = sharpen_lut(ip.bw, ip.bh, ip.sharpen, ip.svr, ip.scutoff);
+  if (ip.degrid_on) t.gs = degrid_sample(ip.bw, ip.bh, ip.degrid, t.win_ana);
+  return t;
+}
+
+// Table `which` (F3D_TAB_*) as a flat float vector; the degrid sample is
+// split into its real and imaginary parts.
+inline std::vector<float> table_of(const PlaneTables& t, int which) {
+  switch (which) {
+  case F3D_TAB_WIN_ANA: return t.win_ana;
+  case F3D_TAB_WIN_SYN_A: return t.syn_a;
+  case F3D_TAB_WIN_SYN_B: return t.syn_b;
+  case F3D_TAB_PATTERN: return t.pattern;
+  case F3D_TAB_SHARPEN: return t.sharpen;
+  case F3D_TAB_GS_RE:
+  case F3D_TAB_GS_IM: {
+    std::vector<float> v;
+    for (size_t i = (which == F3D_TAB_GS_IM); i < t.gs.size(); i += 2) v.push_back(t.gs[i]);
+    return v;
+  }
+  case F3D_TAB_TWIDDLE_ROW: return t.tw_row;
+  case F3D_TAB_TWIDDLE_COL: return t.tw_col;
+  default: return {};
+  }
+}
+
 // CHROMANORM, src/cpu/reference.cpp:70-79: mode-1 YUV chroma only.
 inline float chroma_norm(const f3d_internal_params& p, const f3d_plane_geom& g) {
   if (p.mode != 1 || !g.chroma || g.sample_type == 1) return 0.0f;

@@ -132,6 +132,9 @@ enum {
   F3D_TAB_WIN_ANA = 0, F3D_TAB_WIN_SYN_A, F3D_TAB_WIN_SYN_B, F3D_TAB_PATTERN,
   F3D_TAB_SHARPEN, F3D_TAB_GS_RE, F3D_TAB_GS_IM, F3D_TAB_TWIDDLE_ROW, F3D_TAB_TWIDDLE_COL
 };
+/* The same tables computed on the host without a device (the PlaneRef
+ * constructor, src/cpu/reference.cpp:19-80, and buildDegridSample :172-198). */
+int f3d_compute_table(const f3d_script_params* sp, const f3d_plane_geom* geom, int which, float* dst);
 
 /* GpuRef::forward (src/cl/gpu.cpp:326-347): forward transform of a host float
  * plane (width*height floats, packed), cached as frame fn. */
