@@ -117,9 +117,9 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def make_clip():
+def make_clip(nframes: int = NFRAMES):
     from fft3dcl_gb300 import synth
-    return synth.clip_yuv420p10_luma(W, H, NFRAMES)
+    return synth.clip_yuv420p10_luma(W, H, nframes)
 
 
 # --------------------------------------------------------------- CPU leg --
@@ -174,7 +174,7 @@ def run_reference(args):
     restatement (oracle/), bit-identical to the reference by its tests."""
     import oracle
     oracle.build(ref=False)
-    frames = make_clip()
+    frames = make_clip(args.frames)
     threads = os.cpu_count() or 1
     fps_warm, _ = cpu_steady_state(frames, threads, 0.0, max(1, args.warmup), max(1, args.warmup))
     fps, steps = cpu_steady_state(frames, threads, 0.0, args.steps, args.steps)
@@ -199,7 +199,7 @@ def run_gpu(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    frames = make_clip()
+    frames = make_clip(args.frames)
     clip_dev = torch.from_numpy(np.stack(frames)).to(dev)  # [48, H, W] uint16, resident
     stream = torch.cuda.Stream(device=dev)
     eng = F.Engine(W, H, BITS, form=args.form, device=local_rank, stream=stream.cuda_stream, **PARAMS)
@@ -307,7 +307,7 @@ def run_gpu(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded ramp + moving rectangles, Gaussian noise 12 LSB, 10-bit)",
         "config": {"workload": WORKLOAD, "form": args.form, "parallelism": f"replicas x{world}",
-                   "inputs": "clip resident in HBM (48 x 16.6 MB)",
+                   "inputs": f"clip resident in HBM ({len(frames)} x 16.6 MB)",
                    "l2": "working set per step ~750 MB: four 143 MB window spectra, larger than the 129 MB L2"},
         "kernel_ms": {"forward": round(float(kt[0]), 4), "filter_inverse": inv_ms and round(inv_ms, 4),
                       "overlap_add": round(float(kt[2]), 4)},
@@ -343,6 +343,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="exact", choices=["exact", "fast", "tc"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--frames", type=int, default=NFRAMES,
+                    help="frames of the resident clip (fewer only to keep profiler captures small)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
