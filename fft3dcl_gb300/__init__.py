@@ -93,7 +93,7 @@ EXPORTS = (
     "f3d_forward", "f3d_forward_raw", "f3d_forward_device", "f3d_get_spectra", "f3d_has", "f3d_raw_path",
     "f3d_bytes_per_sample", "f3d_upload_degrid_sample", "f3d_process", "f3d_process_raw",
     "f3d_process_device", "f3d_prune", "f3d_synchronize", "f3d_last_kernel_ms",
-    "f3d_live_instances", "f3d_live_bytes", "f3d_kernel_launches",
+    "f3d_live_instances", "f3d_live_bytes", "f3d_kernel_launches", "f3d_denoise_noalloc",
 )
 
 _lib = None

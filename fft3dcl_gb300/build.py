@@ -51,7 +51,8 @@ def _units():
         obj = os.path.join(BUILD, f"f3d_k_exact_bw{bw}.o")
         units.append((obj, [NVCC] + NVCC_COMMON + NVCC_EXACT + [f"-DF3D_BW={bw}", "-c", src, "-o", obj],
                        [src] + headers))
-    for name, extra in (("f3d_k_common.cu", NVCC_EXACT), ("f3d_k_fast.cu", []), ("f3d_k_tc.cu", [])):
+    for name, extra in (("f3d_k_common.cu", NVCC_EXACT), ("f3d_k_fast.cu", []), ("f3d_k_tc.cu", []),
+                        ("f3d_noalloc.cu", NVCC_EXACT + ["-Xcompiler", "-ffp-contract=off"])):
         src = os.path.join(CSRC, name)
         if not os.path.exists(src):
             continue

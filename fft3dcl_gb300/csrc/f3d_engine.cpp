@@ -41,6 +41,11 @@ int fail_thread(int code, const std::string& msg) {
 
 }  // namespace
 
+namespace f3d {
+// Records the message f3d_last_error returns (for entry points in other files).
+void set_last_error(const char* msg) { t_last_error = msg; }
+}  // namespace f3d
+
 struct f3d_engine {
   std::mutex mtx;
   std::string err;

@@ -186,6 +186,34 @@ size_t f3d_live_bytes(void);
 /* Number of kernel launches made by this library since load (all engines). */
 uint64_t f3d_kernel_launches(void);
 
+/* Denoise one frame without allocating device memory. No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc -- code that
+ * runs while a CUDA graph is being captured, hosts that hand out a fixed
+ * device-memory budget up front, and real-time threads that must not take
+ * cudaMalloc/cudaFree's device-wide synchronisation.
+ *
+ * The caller passes the window frames (`nwin` device pointers in temporal
+ * order, bt of them for bt >= 2, else one; rows `src_pitch` bytes apart) and
+ * the output plane (`dst_pitch`); the work is queued on `stream` (NULL: the
+ * default stream) with the current device's kernels of the exact form, and
+ * the result has the same bits as f3d_forward_device + f3d_process_device.
+ * Spectra, windowed blocks and tables live in one static device array of
+ * F3D_NOALLOC_SCRATCH_BYTES that every GPU that loads this library holds
+ * until the process exits. The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture. All calls share the array and it keeps the
+ * last call's contents; every byte a call reads is written by that call
+ * first. Calls whose work overlaps on a GPU race on the array: order them
+ * (one stream, or events). Kalman (bt=0) needs state across frames and is
+ * refused, as is any plane whose spectra and blocks do not fit the array
+ * (F3D_E_UNSUPPORTED, message says how many bytes it needs). Calls no
+ * cudaMalloc, cudaFree or other allocating routine; host memory is not
+ * allocated either. */
+#define F3D_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
+                        const void* const* dev_window, int nwin, size_t src_pitch, void* dev_dst,
+                        size_t dst_pitch, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
