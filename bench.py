@@ -201,59 +201,74 @@ def run_gpu(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     frames = make_clip(args.frames)
     clip_dev = torch.from_numpy(np.stack(frames)).to(dev)  # [48, H, W] uint16, resident
-    stream = torch.cuda.Stream(device=dev)
-    eng = F.Engine(W, H, BITS, form=args.form, device=local_rank, stream=stream.cuda_stream, **PARAMS)
-    info = eng.info()
     ip = F.validate(W, H, BITS, **PARAMS)
     bt, cur = ip.bt, ip.current
     pitch = W * 2
     out = torch.empty((H, W), dtype=torch.uint16, device=dev)
     nfr = clip_dev.shape[0]
 
-    def step(n):
-        win = [n - cur + i for i in range(bt)]
-        for fn in win:
-            if not eng.has(fn):
-                eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
-        eng.process_device(win, out.data_ptr(), pitch)
-        eng.prune(n - cur - 1, n - cur + bt)
-
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    n = cur
-    for _ in range(max(3, args.warmup)):
-        step(n)
-        n += 1
-    torch.cuda.synchronize(dev)
+    def device_run(form, with_clocks=False):
+        """Steady-state steps with the clip resident in HBM: (ms for
+        args.steps steps, per-kernel ms, launches, clocks, engine)."""
+        stream = torch.cuda.Stream(device=dev)
+        eng = F.Engine(W, H, BITS, form=form, device=local_rank, stream=stream.cuda_stream, **PARAMS)
 
-    clocks = Clocks(local_rank)
-    clocks.start()
-    barrier()
-    torch.cuda.synchronize(dev)
-    l0 = F.kernel_launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step(n)
-        n += 1
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    barrier()
-    launches = F.kernel_launches() - l0
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
+        def step(n):
+            win = [n - cur + i for i in range(bt)]
+            for fn in win:
+                if not eng.has(fn):
+                    eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
+            eng.process_device(win, out.data_ptr(), pitch)
+            eng.prune(n - cur - 1, n - cur + bt)
 
-    # Per-kernel device time over the same number of steps (a synchronize
-    # after each step so that the engine's events can be read).
-    kt = np.zeros(3)
-    for _ in range(args.steps):
-        step(n)
-        n += 1
-        eng.synchronize()
-        kt += np.array(eng.last_kernel_ms())
-    kt /= args.steps
+        n = cur
+        for _ in range(max(3, args.warmup)):
+            step(n)
+            n += 1
+        torch.cuda.synchronize(dev)
+        clocks = Clocks(local_rank) if with_clocks else None
+        if clocks:
+            clocks.start()
+        barrier()
+        torch.cuda.synchronize(dev)
+        l0 = F.kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(n)
+            n += 1
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        launches = F.kernel_launches() - l0
+        clk = clocks.stop() if clocks else None
+        ms = e0.elapsed_time(e1)
+        # Per-kernel device time over the same number of steps (a synchronize
+        # after each step so that the engine's events can be read).
+        kt = np.zeros(3)
+        for _ in range(args.steps):
+            step(n)
+            n += 1
+            eng.synchronize()
+            kt += np.array(eng.last_kernel_ms())
+        kt /= args.steps
+        return ms, kt, launches, clk, eng, stream, n
+
+    # Other forms first (device throughput only), then the headline form.
+    forms = {}
+    for f in [x for x in args.compare.split(",") if x and x != args.form]:
+        ms_f, kt_f, _, _, eng_f, _, _ = device_run(f)
+        forms[f] = {"value": round(args.steps * world / (ms_f / 1000.0), 3),
+                    "kernel_ms": [round(float(x), 4) for x in kt_f]}
+        eng_f.close()
+    ms, kt, launches, clk, eng, stream, n = device_run(args.form, with_clocks=True)
+    info = eng.info()
+    forms[args.form] = {"value": round(args.steps * world / (ms / 1000.0), 3),
+                        "kernel_ms": [round(float(x), 4) for x in kt]}
 
     # End to end through the C ABI with host buffers: pinned source planes,
     # upload of the entering frame and readback of the packed output.
@@ -300,7 +315,11 @@ def run_gpu(args, rank, world, local_rank):
     ab = algorithmic_bytes(info.nblocks, info.fbw, ip.bh, bt)
     peak, peak_kind = load_peaks()
     inv_ms = float(kt[1])
-    achieved = ab["filter_inverse"] / (inv_ms / 1000.0) / 1e9 if inv_ms > 0 else None
+    # The dominant kernel: the fused sweep (window spectra in, packed plane
+    # out) or, unfused, the filter+inverse kernel (window spectra in).
+    kname = "k_sweep (filter+inverse+overlap-add+pack)" if info.fused else "k_inverse (filter+inverse)"
+    kbytes = ab["filter_inverse"] + (ab["plane"] if info.fused else 0)
+    achieved = kbytes / (inv_ms / 1000.0) / 1e9 if inv_ms > 0 else None
     line = {
         "metric": METRIC, "value": round(fps, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
@@ -311,10 +330,11 @@ def run_gpu(args, rank, world, local_rank):
                    "l2": "working set per step ~750 MB: four 143 MB window spectra, larger than the 129 MB L2"},
         "kernel_ms": {"forward": round(float(kt[0]), 4), "filter_inverse": inv_ms and round(inv_ms, 4),
                       "overlap_add": round(float(kt[2]), 4)},
-        "roofline": {"kernel": "filter_inverse", "bound": "hbm",
+        "forms": forms,
+        "roofline": {"kernel": kname, "bound": "hbm",
                      "achieved": achieved and round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": achieved and round(achieved / peak, 4),
-                     "traffic": NCU_TRAFFIC.get(args.form), "algorithmic_bytes": ab["filter_inverse"],
+                     "traffic": NCU_TRAFFIC.get(args.form), "algorithmic_bytes": kbytes,
                      "peak_source": f"{peak_kind} hbm_gbs"},
         "roofline_step": {"algorithmic_bytes": ab["frame"],
                           "achieved": round(ab["frame"] * fps / world / 1e9, 1), "unit": "GB/s",
@@ -341,7 +361,10 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="exact", choices=["exact", "fast", "tc"])
+    ap.add_argument("--form", default="fast", choices=["exact", "fast", "tc"],
+                    help="arithmetic form of the headline line")
+    ap.add_argument("--compare", default="exact,fast",
+                    help="comma-separated forms whose device throughput is reported under 'forms'")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--frames", type=int, default=NFRAMES,
                     help="frames of the resident clip (fewer only to keep profiler captures small)")

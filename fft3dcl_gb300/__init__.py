@@ -75,14 +75,18 @@ class PlaneGeom(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("device", C.c_int), ("form", C.c_int), ("stream", C.c_void_p)]
+    _fields_ = [("device", C.c_int), ("form", C.c_int), ("stream", C.c_void_p), ("flags", C.c_int)]
+
+
+FLAG_UNFUSED, FLAG_PREFETCH_EARLY, FLAG_PREFETCH_LATE = 1, 2, 4
 
 
 class EngineInfo(C.Structure):
     _fields_ = [("nblocks", C.c_int), ("fbw", C.c_int), ("ncols", C.c_int), ("nrows", C.c_int),
                 ("bytes_per_sample", C.c_int), ("raw_path", C.c_int),
                 ("spectrum_bytes", C.c_size_t), ("device_bytes", C.c_size_t),
-                ("cached_frames", C.c_int), ("chroma_norm", C.c_float)]
+                ("cached_frames", C.c_int), ("chroma_norm", C.c_float), ("form", C.c_int),
+                ("fused", C.c_int)]
 
 
 # Every symbol the C ABI declares (include/fft3d_gb300.h).
@@ -233,11 +237,11 @@ class Engine:
 
     def __init__(self, width: int, height: int, bits: int = 8, sample_type: int = 0,
                  chroma: bool = False, form: str = "exact", device: int = 0, stream: int | None = None,
-                 **params):
+                 fused: bool = True, flags: int = 0, **params):
         self.sp = script_params(**params)
         self.geom = PlaneGeom(width, height, bits, sample_type, int(chroma))
         self.width, self.height, self.bits, self.sample_type = width, height, bits, sample_type
-        opts = Options(device, FORMS[form], stream or None)
+        opts = Options(device, FORMS[form], stream or None, flags | (0 if fused else FLAG_UNFUSED))
         h = C.c_void_p()
         if lib().f3d_engine_create(C.byref(self.sp), C.byref(self.geom), C.byref(opts),
                                    C.byref(h)) != F3D_OK:
@@ -372,7 +376,7 @@ class Filter:
     order, as the reference's fmFrameState mode delivers them."""
 
     def __init__(self, clip, fmt: VideoFormat, form: str = "exact", device: int = 2,
-                 gpu: int = 0, **params):
+                 gpu: int = 0, fused: bool = True, **params):
         if fmt.sample_type == 1 and fmt.bits != 32:
             raise ValueError("FFT3DCL: only 32-bit float clips supported (16-bit float not ported yet)")
         if fmt.sample_type == 0 and not 8 <= fmt.bits <= 16:
@@ -409,7 +413,7 @@ class Filter:
                 h, w = first[p].shape
                 self.engines.append(Engine(w, h, fmt.bits, fmt.sample_type,
                                            chroma=(fmt.color_family == "yuv" and p > 0),
-                                           form=form, device=gpu, **params))
+                                           form=form, device=gpu, fused=fused, **params))
         except Exception:
             self.close()
             raise

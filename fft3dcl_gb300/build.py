@@ -36,6 +36,8 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # Exact form: no fused multiply-add, IEEE division and square root, no
 # flush-to-zero -- every fp32 operation rounds like the reference CPU code.
 NVCC_EXACT = ["--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
+# Fast and tensor-core forms: FMA and the hardware reciprocal / square root.
+NVCC_FAST = ["--fmad=true", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"]
 # Host code builds the tables the kernels read; GCC fuses multiply-adds in
 # C++ by default on aarch64, which would change their last bits there.
 HOST_CXX = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-ffp-contract=off"]
@@ -51,7 +53,8 @@ def _units():
         obj = os.path.join(BUILD, f"f3d_k_exact_bw{bw}.o")
         units.append((obj, [NVCC] + NVCC_COMMON + NVCC_EXACT + [f"-DF3D_BW={bw}", "-c", src, "-o", obj],
                        [src] + headers))
-    for name, extra in (("f3d_k_common.cu", NVCC_EXACT), ("f3d_k_fast.cu", []), ("f3d_k_tc.cu", []),
+    for name, extra in (("f3d_k_common.cu", NVCC_EXACT), ("f3d_k_fast.cu", NVCC_FAST),
+                        ("f3d_k_sweep.cu", NVCC_FAST), ("f3d_k_tc.cu", NVCC_FAST),
                         ("f3d_noalloc.cu", NVCC_EXACT + ["-Xcompiler", "-ffp-contract=off"])):
         src = os.path.join(CSRC, name)
         if not os.path.exists(src):

@@ -92,11 +92,17 @@ __device__ __forceinline__ void wienner(float& re, float& im, float sx, float sy
   im *= mul;
 }
 
+// Temporal mode as a template argument: -1..4 fixed at compile time (no
+// branch, and no Kalman state stores in the other modes' code, so the
+// compiler may move spectra loads freely), kRuntimeBm to read a.bm.
+constexpr int kRuntimeBm = -2;
+
 // Temporal filter + sharpen of bin i (0 <= i < bh*fbw) of block b, with
 // gi = b*bh*fbw + i. Follows src/cpu/reference.cpp:229-409 per bin:
 // degrid correction, bm 2/3/4 temporal DFT + Wiener, bm 1 Wiener, bm 0
 // Kalman (state updated in place), bm -1 pass-through, then sharpen.
-__device__ __forceinline__ float2 filter_bin(const InvArgs& a, int b, int i, size_t gi) {
+template <int BM>
+__device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, int b, int i, size_t gi) {
   float d_re = 0.0f, d_im = 0.0f;
   if (a.dg) {
     const size_t ps = (size_t)a.g.bh * a.g.fbw;
@@ -112,7 +118,7 @@ __device__ __forceinline__ float2 filter_bin(const InvArgs& a, int b, int i, siz
     sy = pv;
   }
   float fr, fi;
-  const int bm = a.bm;
+  const int bm = BM == kRuntimeBm ? a.bm : BM;
   if (bm == 2) {
     const float2 p = a.s[0][gi], c = a.s[1][gi];
     float ar = c.x - p.x, ai = c.y - p.y;
@@ -245,6 +251,10 @@ __device__ __forceinline__ float2 filter_bin(const InvArgs& a, int b, int i, siz
     fi = im;
   }
   return make_float2(fr, fi);
+}
+
+__device__ __forceinline__ float2 filter_bin(const InvArgs& a, int b, int i, size_t gi) {
+  return filter_bin_t<kRuntimeBm>(a, b, i, gi);
 }
 
 // One radix-2 DIT stage of length LEN over N register values: butterflies

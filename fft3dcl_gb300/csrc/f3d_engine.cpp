@@ -76,6 +76,12 @@ struct f3d_engine {
   float* d_kproc = nullptr;
   bool kalman_first = true;
 
+  // Fused sweep (mode 1, half overlap): CTA grid and seam scratch.
+  bool fused = false;
+  int sweep_strips = 0, sweep_segs = 0, sweep_prefetch = 0;
+  float* d_seam = nullptr;
+  size_t seam_floats = 0;
+
   size_t bytes = 0;
   // Kernel timing on the engine stream: forward [0,1], filter+inverse [2,4],
   // overlap-add [4,3].
@@ -229,6 +235,32 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
   a.ssmax = e->ip.ssmax;
   a.kalman_cn = e->ip.kalman_cn;
   a.kr2 = e->ip.kratio * e->ip.kratio;
+  if (e->fused) {
+    // One fused launch (plus the seam merge) writes the packed plane.
+    SweepArgs sa{};
+    sa.inv = a;
+    sa.dst = ddst;
+    sa.pitch = pitch;
+    sa.fmt = fmt;
+    sa.chroma_norm = e->cnorm;
+    sa.inv_norm = e->inv_norm;
+    sa.max_pix = e->max_pix;
+    sa.cells_x = (a.g.W + a.g.bw / 2 - 1) / (a.g.bw / 2);
+    sa.cells_y = (a.g.H + a.g.bh / 2 - 1) / (a.g.bh / 2);
+    sa.strips = e->sweep_strips;
+    sa.segs = e->sweep_segs;
+    sa.seam_w = sa.cells_x * (a.g.bw / 2);
+    sa.seam_b = e->d_seam;
+    sa.seam_t = e->d_seam ? e->d_seam + (size_t)(sa.segs - 1) * (a.g.bh / 2) * sa.seam_w : nullptr;
+    sa.prefetch = e->sweep_prefetch;
+    cudaEventRecord(e->ev[2], e->stream);
+    cudaError_t ce = launch_sweep(e->form, sa, e->stream);
+    cudaEventRecord(e->ev[4], e->stream);
+    cudaEventRecord(e->ev[3], e->stream);
+    e->proc_timed = true;
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "the fused filter/inverse/overlap-add launch");
+    return F3D_OK;
+  }
   cudaEventRecord(e->ev[2], e->stream);
   cudaError_t ce = launch_filter_inverse(e->form, a, e->stream);
   cudaEventRecord(e->ev[4], e->stream);
@@ -306,8 +338,13 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
   f3d_internal_params ip;
   std::string err;
   if (!validate_params(*sp, g.width, g.height, g.bits, ip, &err)) return fail_thread(F3D_E_PARAM, err);
-  const int form = opts ? opts->form : F3D_FORM_EXACT;
+  int form = opts ? opts->form : F3D_FORM_EXACT;
   const int device = opts ? opts->device : 0;
+  if (form < F3D_FORM_EXACT || form > F3D_FORM_TC) return fail_thread(F3D_E_PARAM, "FFT3DCL: unknown form");
+  // Kalman's reset is a threshold on per-bin frame differences: any rounding
+  // difference flips bins near it, so bt=0 runs the exact kernels in every
+  // form. Blocks the faster forms do not cover (4-wide) use them too.
+  if (ip.bm == 0 || !form_supported(form, ip.bw, ip.bh)) form = F3D_FORM_EXACT;
   if (!form_supported(form, ip.bw, ip.bh))
     return fail_thread(F3D_E_UNSUPPORTED,
                        "FFT3DCL: block size " + std::to_string(ip.bw) + "x" + std::to_string(ip.bh) +
@@ -402,6 +439,18 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
         (ce = e->alloc(&e->d_kproc, sizeof(float) * nbin)) != cudaSuccess)
       return finish_fail(e->cuda_fail(ce, "Kalman state allocation"));
   }
+  const Geo geo = make_geo(e);
+  if (!(opts && (opts->flags & F3D_FLAG_UNFUSED)) && sweep_supported(form, geo, ip.bm)) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    sweep_plan(geo, sms > 0 ? sms : 1, &e->sweep_strips, &e->sweep_segs);
+    e->seam_floats = sweep_seam_floats(geo, e->sweep_segs);
+    if (e->seam_floats && (ce = e->alloc(&e->d_seam, sizeof(float) * e->seam_floats)) != cudaSuccess)
+      return finish_fail(e->cuda_fail(ce, "seam buffer allocation"));
+    e->fused = true;
+    const int fl = opts ? opts->flags : 0;
+    e->sweep_prefetch = (fl & F3D_FLAG_PREFETCH_EARLY) ? 1 : (fl & F3D_FLAG_PREFETCH_LATE) ? 2 : 0;
+  }
   *out = e;
   return F3D_OK;
 }
@@ -429,6 +478,7 @@ void f3d_engine_destroy(f3d_engine* e) {
     e->release(e->d_klast, sizeof(float2) * nbin);
     e->release(e->d_kcov, sizeof(float) * nbin);
     e->release(e->d_kproc, sizeof(float) * nbin);
+    e->release(e->d_seam, sizeof(float) * e->seam_floats);
     for (auto& ev : e->ev)
       if (ev) cudaEventDestroy(ev);
     if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
@@ -452,6 +502,8 @@ int f3d_engine_get_info(f3d_engine* e, f3d_engine_info* info) {
   info->device_bytes = e->bytes;
   info->cached_frames = (int)e->cache.size();
   info->chroma_norm = e->cnorm;
+  info->form = e->form;
+  info->fused = e->fused ? 1 : 0;
   return F3D_OK;
 }
 

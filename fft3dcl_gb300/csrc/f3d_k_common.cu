@@ -73,10 +73,12 @@ static bool pow2_in(int v, int lo, int hi) { return v >= lo && v <= hi && (v & (
 
 bool form_supported(int form, int bw, int bh) {
   if (form == F3D_FORM_EXACT) return pow2_in(bw, 4, 64) && pow2_in(bh, 4, 64);
+  if (form == F3D_FORM_FAST) return pow2_in(bw, 8, 64) && pow2_in(bh, 8, 64);
   return false;
 }
 
 cudaError_t launch_forward(int form, const FwdArgs& a, cudaStream_t st) {
+  if (form == F3D_FORM_FAST) return launch_forward_fast(a, st);
   if (form != F3D_FORM_EXACT) return cudaErrorNotSupported;
   switch (a.g.bw) {
   case 4: return launch_forward_exact_bw4(a, st);
@@ -89,6 +91,7 @@ cudaError_t launch_forward(int form, const FwdArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_filter_inverse(int form, const InvArgs& a, cudaStream_t st) {
+  if (form == F3D_FORM_FAST) return launch_inverse_fast(a, st);
   if (form != F3D_FORM_EXACT) return cudaErrorNotSupported;
   switch (a.g.bw) {
   case 4: return launch_inverse_exact_bw4(a, st);

@@ -1,0 +1,229 @@
+// f3d_k_sweep.cu -- fused filter + inverse + overlap-add + packing (fast
+// form) for mode 1 with half overlap, the geometry of every default and
+// benchmark configuration.
+//
+// Cells: the plane is cut into cells of cw x ch = (bw/2) x (bh/2) samples;
+// block (m, n) covers cell rows m-1, m and cell columns n-1, n, so cell (i, j)
+// is the sum of four quadrants, taken in the reference's block order
+// (src/cpu/reference.cpp:415-430):
+//   ((q(i,j) + q(i,j+1)) + q(i+1,j)) + q(i+1,j+1)
+// where q(m,n) is the part of block (m, n)'s windowed inverse over the cell.
+// With half overlap every cell inside the plane has all four blocks.
+//
+// A CTA of 256 threads holds 256/TPB block slots; it owns a strip of
+// TJ = slots-1 cells (slot s computes block column J0+s, the last slot the
+// strip's right neighbour column) and a segment [M0, M1) of block rows. For
+// each block row m it filters and inverts the row's blocks into shared
+// memory, then
+//   - finishes cell row m-1 from the partial sums P (q(m-1,j) + q(m-1,j+1))
+//     plus the top halves of row m, and writes it, packed, to the plane;
+//   - starts cell row m: P = bottom halves of row m.
+// The first cell row of a segment (row M0-1) and its last (M1-1) are shared
+// with the neighbouring segments: their quadrants go to seam buffers and
+// k_seam_merge finishes them in the same order. The next row's window
+// spectra can be bulk-prefetched into L2 while row m is processed (off by
+// default: with one wave of CTAs each holding a row, the prefetched rows
+// exceed what L2 keeps and the extra traffic costs more than it hides).
+#include "f3d_fast.cuh"
+
+namespace f3d {
+namespace {
+
+constexpr int kSweepThreads = 256;
+
+template <int BW, int BH>
+struct SCfg {
+  using C = FCfg<BW, BH>;
+  static constexpr int TPB = C::TPB;
+  static constexpr int SLOTS = kSweepThreads / TPB;
+  static constexpr int TJ = SLOTS - 1;             // cells per strip
+  static constexpr int CW = BW / 2, CH = BH / 2;   // cell size
+  static constexpr int QK = CW / 4;                // float4 chunks per cell row
+  static constexpr size_t SMEM = sizeof(float2) * C::SMEM_F2 * SLOTS + sizeof(float) * TJ * CH * CW;
+};
+
+// Samples x..x+3 (x even) of row y of a block's windowed inverse, stored in
+// its tile as pairs: (x, x+1) at Q[(x/2)*SB + yperm(y)].
+template <int SB, int BH>
+__device__ __forceinline__ float4 qload(const float2* Q, int y, int x) {
+  const int yp = yperm<BH>(y);
+  const float2 lo = Q[(x / 2) * SB + yp], hi = Q[(x / 2 + 1) * SB + yp];
+  return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+__device__ __forceinline__ float4 add4(float4 a, float4 b) {
+  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+// Four output samples at x..x+3 of row y (bounds-checked against the plane).
+__device__ __forceinline__ void store4(const SweepArgs& sa, int y, int x, float4 v) {
+  if (y >= sa.inv.g.H) return;
+  uint8_t* row = sa.dst + (long long)y * sa.pitch;
+  const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    if (x + k >= sa.inv.g.W) break;
+    float s = e[k];
+    if (sa.chroma_norm != 0.0f) s += sa.chroma_norm;
+    store_sample(row, x + k, s, sa.fmt, sa.inv_norm, sa.max_pix);
+  }
+}
+
+template <int BW, int BH, int BM>
+__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep_fast(const __grid_constant__ SweepArgs sa) {
+  using S_ = SCfg<BW, BH>;
+  using C = FCfg<BW, BH>;
+  constexpr int TPB = S_::TPB, TJ = S_::TJ, CW = S_::CW, CH = S_::CH, QK = S_::QK;
+  constexpr int NWIN = BM >= 2 ? BM : 1;
+  const InvArgs& a = sa.inv;
+  extern __shared__ float4 smem4[];
+  float2* slots = reinterpret_cast<float2*>(smem4);
+  float4* P = reinterpret_cast<float4*>(slots + S_::SLOTS * C::SMEM_F2);  // [TJ][CH][QK]
+  const int slot = threadIdx.x / TPB, t = threadIdx.x - slot * TPB;
+  float2* S = slots + slot * C::SMEM_F2;
+  const int strip = blockIdx.x % sa.strips, seg = blockIdx.x / sa.strips;
+  const int J0 = strip * TJ;
+  const int nrow = sa.cells_y + 1;  // block rows 0..cells_y are needed
+  const int M0 = (int)((long long)seg * nrow / sa.segs);
+  const int M1 = (int)((long long)(seg + 1) * nrow / sa.segs);
+  const int n = J0 + slot;
+  const bool col_ok = n <= sa.cells_x;  // block columns 0..cells_x are needed
+  const int ncell = min(TJ, sa.cells_x - J0);
+  constexpr float inv_n = 1.0f / (BW * BH);
+
+  // L2 prefetch of one block's window spectra (one thread per slot).
+  auto prefetch_block = [&](int bb) {
+#pragma unroll
+    for (int k = 0; k < NWIN; k++) prefetch_l2(a.s[k] + (size_t)bb * C::PS, C::PS * sizeof(float2));
+  };
+  if (sa.prefetch && t == 0 && col_ok && M0 < M1) prefetch_block(M0 * a.g.ncols + n);
+  for (int m = M0; m < M1; m++) {
+    const int b = m * a.g.ncols + n;
+    const bool pf_next = t == 0 && col_ok && m + 1 < M1;
+    if (sa.prefetch == 1 && pf_next) prefetch_block(b + a.g.ncols);
+    // Windowed rows go back into the tile as sample pairs: (x, x+1) of row y
+    // at S[(x/2)*SB + yperm(y)] (see inverse_block).
+    const float* win = (n & 1) ? a.win_b : a.win_a;
+    inverse_block<BW, BH, BM>(a, b, t, col_ok, S, [&](int y, const float2(&xy)[BW / 2]) {
+#pragma unroll
+      for (int k = 0; k < BW / 2; k++) {
+        const float2 wv = *reinterpret_cast<const float2*>(win + y * BW + 2 * k);
+        S[k * C::SB + yperm<BH>(y)] = make_float2(xy[k].x * inv_n * wv.x, xy[k].y * inv_n * wv.y);
+      }
+    }, [&] {
+      // Row m's spectra are read by now: fetch row m+1 while the transforms
+      // and the cell sums of row m run.
+      if (sa.prefetch == 2 && pf_next) prefetch_block(b + a.g.ncols);
+    });
+    __syncthreads();
+    const bool emit = m > M0;                       // cell row m-1 finishes here
+    const bool seam_top = m == M0 && M0 > 0;        // cell row M0-1: quadrants 3, 4 to the seam
+    const bool seam_bot = m == M1 - 1 && seg < sa.segs - 1;  // cell row M1-1: quadrants 1, 2
+    for (int it = threadIdx.x; it < CH * TJ * QK; it += kSweepThreads) {
+      const int yy = it / (TJ * QK);
+      const int rem = it - yy * (TJ * QK);
+      const int jj = rem / QK, k = rem - jj * QK;
+      if (jj >= ncell) continue;
+      const float2* Qa = slots + jj * C::SMEM_F2;
+      const float2* Qb = slots + (jj + 1) * C::SMEM_F2;
+      const float4 q10 = qload<C::SB, BH>(Qa, yy, CW + 4 * k);  // block (m, j) top right
+      const float4 q11 = qload<C::SB, BH>(Qb, yy, 4 * k);       // block (m, j+1) top left
+      float4& p = P[(jj * CH + yy) * QK + k];
+      const int x = (J0 + jj) * CW + 4 * k;
+      if (emit) {
+        store4(sa, (m - 1) * CH + yy, x, add4(add4(p, q10), q11));
+      } else if (seam_top) {
+        float* t0 = sa.seam_t + ((size_t)((seg - 1) * 2) * CH + yy) * sa.seam_w + x;
+        float* t1 = sa.seam_t + ((size_t)((seg - 1) * 2 + 1) * CH + yy) * sa.seam_w + x;
+        *reinterpret_cast<float4*>(t0) = q10;
+        *reinterpret_cast<float4*>(t1) = q11;
+      }
+      p = add4(qload<C::SB, BH>(Qa, CH + yy, CW + 4 * k), qload<C::SB, BH>(Qb, CH + yy, 4 * k));  // row m bottom halves
+      if (seam_bot) *reinterpret_cast<float4*>(sa.seam_b + ((size_t)seg * CH + yy) * sa.seam_w + x) = p;
+    }
+    __syncthreads();
+  }
+}
+
+// Finishes the seam cell rows: ((q1 + q2) + q3) + q4 per sample, packed.
+__global__ void __launch_bounds__(256) k_seam_merge(const __grid_constant__ SweepArgs sa, int ch) {
+  const int x = blockIdx.x * 256 + threadIdx.x;
+  const int yy = blockIdx.y, k = blockIdx.z;  // seam k: cell row M1(k) - 1
+  if (x >= sa.inv.g.W) return;
+  const int nrow = sa.cells_y + 1;
+  const int m1 = (int)((long long)(k + 1) * nrow / sa.segs);
+  const int y = (m1 - 1) * ch + yy;
+  if (y >= sa.inv.g.H) return;
+  const size_t o = ((size_t)k * ch + yy) * sa.seam_w + x;
+  const size_t ot = ((size_t)(k * 2) * ch + yy) * sa.seam_w + x;
+  float v = sa.seam_b[o] + sa.seam_t[ot];
+  v = v + sa.seam_t[ot + (size_t)ch * sa.seam_w];
+  if (sa.chroma_norm != 0.0f) v += sa.chroma_norm;
+  store_sample(sa.dst + (long long)y * sa.pitch, x, v, sa.fmt, sa.inv_norm, sa.max_pix);
+}
+
+template <int BW, int BH, int BM>
+cudaError_t launch_bm(const SweepArgs& a, cudaStream_t st) {
+  using S_ = SCfg<BW, BH>;
+  auto k = k_sweep_fast<BW, BH, BM>;
+  static_assert(S_::SMEM <= 110 * 1024, "two CTAs per SM");
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_::SMEM);
+  if (e != cudaSuccess) return e;
+  k<<<a.strips * a.segs, kSweepThreads, S_::SMEM, st>>>(a);
+  count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess || a.segs < 2) return e;
+  dim3 grid((a.inv.g.W + 255) / 256, BH / 2, a.segs - 1);
+  k_seam_merge<<<grid, 256, 0, st>>>(a, BH / 2);
+  count_launch();
+  return cudaGetLastError();
+}
+
+template <int BW, int BH>
+cudaError_t launch_size(const SweepArgs& a, cudaStream_t st) {
+  switch (a.inv.bm) {
+  case -1: return launch_bm<BW, BH, -1>(a, st);
+  case 1: return launch_bm<BW, BH, 1>(a, st);
+  case 2: return launch_bm<BW, BH, 2>(a, st);
+  case 3: return launch_bm<BW, BH, 3>(a, st);
+  case 4: return launch_bm<BW, BH, 4>(a, st);
+  default: return cudaErrorNotSupported;
+  }
+}
+
+}  // namespace
+
+bool sweep_supported(int form, const Geo& g, int bm) {
+  if (form != F3D_FORM_FAST || bm == 0 || g.mode != 1) return false;
+  if (g.bw != g.bh || (g.bw != 8 && g.bw != 16 && g.bw != 32)) return false;
+  return g.xoff == -g.bw / 2 && g.xstep == g.bw / 2 && g.yoff == -g.bh / 2 && g.ystep == g.bh / 2;
+}
+
+void sweep_plan(const Geo& g, int sm_count, int* strips, int* segs) {
+  const int tpb = g.bw / 2, tj = kSweepThreads / tpb - 1;
+  const int cells_x = (g.W + g.bw / 2 - 1) / (g.bw / 2);
+  const int cells_y = (g.H + g.bh / 2 - 1) / (g.bh / 2);
+  *strips = (cells_x + tj - 1) / tj;
+  // One wave of two CTAs per SM, segments of at least two block rows.
+  int s = (2 * sm_count + *strips - 1) / *strips;
+  const int maxseg = (cells_y + 1) / 2;
+  if (s > maxseg) s = maxseg;
+  *segs = s < 1 ? 1 : s;
+}
+
+size_t sweep_seam_floats(const Geo& g, int segs) {
+  const int cells_x = (g.W + g.bw / 2 - 1) / (g.bw / 2);
+  return (size_t)(segs > 1 ? segs - 1 : 0) * 3 * (g.bh / 2) * (size_t)cells_x * (g.bw / 2);
+}
+
+cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st) {
+  if (!sweep_supported(form, a.inv.g, a.inv.bm)) return cudaErrorNotSupported;
+  switch (a.inv.g.bw) {
+  case 8: return launch_size<8, 8>(a, st);
+  case 16: return launch_size<16, 16>(a, st);
+  case 32: return launch_size<32, 32>(a, st);
+  default: return cudaErrorNotSupported;
+  }
+}
+
+}  // namespace f3d

@@ -70,6 +70,35 @@ struct OlaArgs {
   float chroma_norm, inv_norm, max_pix;
 };
 
+// Fused filter + inverse + overlap-add + packing for mode 1 with half
+// overlap (bw = 2 ow, bh = 2 oh), the "sweep": the plane is cut into cells of
+// (bw/2) x (bh/2) samples, each covered by exactly four blocks. A CTA owns a
+// strip of cells and a range of block rows (a segment); it sweeps down the
+// block rows, adding each row's windowed blocks to the cells in shared
+// memory in the reference's block order, and writes finished cells straight
+// to the output plane. Cell rows on the boundary between two segments are
+// finished by a merge pass from the seam buffers.
+struct SweepArgs {
+  InvArgs inv;
+  uint8_t* dst;          // output plane
+  long long pitch;
+  int fmt;
+  float chroma_norm, inv_norm, max_pix;
+  int cells_x, cells_y;  // cells covering the plane
+  int strips, segs;      // CTA (strip, segment) grid
+  int seam_w;            // floats per seam row (cells_x * bw/2)
+  int prefetch;          // L2 prefetch of the next block row: 0 off, 1 at row start, 2 after the filter
+  float* seam_b;         // [segs-1][bh/2][seam_w]: first two quadrants of each seam cell, summed
+  float* seam_t;         // [segs-1][2][bh/2][seam_w]: third and fourth quadrants
+};
+
+// Whether the sweep handles this geometry and form; its CTA grid; the seam
+// scratch it needs (floats); and the launches (sweep, then merge).
+bool sweep_supported(int form, const Geo& g, int bm);
+void sweep_plan(const Geo& g, int sm_count, int* strips, int* segs);
+size_t sweep_seam_floats(const Geo& g, int segs);
+cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st);
+
 // Kernel launches; each returns the launch error. `form` is F3D_FORM_*.
 cudaError_t launch_forward(int form, const FwdArgs& a, cudaStream_t st);
 cudaError_t launch_filter_inverse(int form, const InvArgs& a, cudaStream_t st);
@@ -87,6 +116,10 @@ F3D_DECLARE_EXACT(16)
 F3D_DECLARE_EXACT(32)
 F3D_DECLARE_EXACT(64)
 #undef F3D_DECLARE_EXACT
+
+// Fast-form launchers (f3d_k_fast.cu); spectra are column-major per block.
+cudaError_t launch_forward_fast(const FwdArgs& a, cudaStream_t st);
+cudaError_t launch_inverse_fast(const InvArgs& a, cudaStream_t st);
 
 // Counts one kernel launch made by this library (all engines, all threads).
 void count_launch();

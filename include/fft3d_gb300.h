@@ -90,7 +90,17 @@ typedef struct {
   int device;   /* CUDA device ordinal                                   */
   int form;     /* F3D_FORM_*                                            */
   void* stream; /* cudaStream_t to run on, NULL: the engine makes one    */
+  int flags;    /* F3D_FLAG_*                                            */
 } f3d_options;
+
+/* Run filter/inverse and overlap-add as separate kernels even where the
+ * fused sweep kernel applies (for comparisons). */
+#define F3D_FLAG_UNFUSED 1
+/* Sweep tuning: bulk-prefetch the next block row's spectra into L2 when a
+ * row starts, or once the row's spectra are read. Off by default (measured
+ * at 4K 10-bit bt=4: off 0.288 ms, late 0.292 ms, early 0.322 ms). */
+#define F3D_FLAG_PREFETCH_EARLY 2
+#define F3D_FLAG_PREFETCH_LATE 4
 
 typedef struct {
   int nblocks, fbw, ncols, nrows;
@@ -100,6 +110,9 @@ typedef struct {
   size_t device_bytes;   /* all device memory held by the engine */
   int cached_frames;
   float chroma_norm;
+  int form; /* form the engine runs: Kalman (bt=0) and 4-wide blocks run
+               F3D_FORM_EXACT whatever was asked */
+  int fused; /* filter, inverse, overlap-add and packing run as one kernel */
 } f3d_engine_info;
 
 typedef struct f3d_engine f3d_engine;

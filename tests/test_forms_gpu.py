@@ -1,0 +1,102 @@
+"""GPU parity of the non-exact arithmetic forms against the oracle.
+
+Tolerances (the ones the path is specified with): +-1 LSB for 8-bit output,
++-4 LSB for 10-bit output (10-bit samples in 16-bit words), 1e-4 absolute for
+float output with samples in [0, 1]. Each case also checks run-to-run
+determinism of the form."""
+import numpy as np
+import pytest
+
+import fft3dcl_gb300 as F
+import oracle
+from fft3dcl_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+FORMS = ["fast"]
+
+
+def tol_for(frames, bits):
+    if frames[0].dtype == np.float32:
+        return 1e-4
+    return 1 if bits <= 8 else 4
+
+
+def run(frames, bits, form, **params):
+    return F.FFT3DCL(frames, bits=bits, form=form, **params)
+
+
+def check(got, ref, tol):
+    worst = 0.0
+    for g, r in zip(got, ref):
+        d = np.abs(g.astype(np.float64) - r.astype(np.float64)).max()
+        worst = max(worst, d)
+    assert worst <= tol, f"max |diff| {worst} > {tol}"
+    return worst
+
+
+CASES = [
+    ("gray8_bt3", lambda: synth.clip_gray8(frames=8), 8, dict(bt=3)),
+    ("gray8_bt4_sharpen", lambda: synth.clip_gray8(frames=6), 8, dict(bt=4, sharpen=0.4)),
+    ("gray8_bt2_beta", lambda: synth.clip_gray8(frames=5), 8, dict(bt=2, beta=1.5, degrid=0.5)),
+    ("gray8_bt1_pattern", lambda: synth.clip_gray8(frames=3), 8,
+     dict(bt=1, sigma2=1.0, sigma3=3.0, sigma4=4.0)),
+    ("gray8_btm1", lambda: synth.clip_gray8(frames=2), 8, dict(bt=-1, sharpen=0.7)),
+    ("gray8_bw16_wintype1", lambda: synth.clip_gray8(frames=5), 8, dict(bw=16, bh=16, wintype=1)),
+    ("gray8_bw8x64_overlap", lambda: synth.clip_gray8(frames=5), 8, dict(bw=8, bh=64, ow=2, oh=16)),
+    ("gray8_mode0", lambda: synth.clip_gray8(frames=5), 8, dict(mode=0, bw=16, bh=32)),
+    ("p10_4k_bt4", lambda: synth.clip_yuv420p10_luma(frames=5), 10, dict(sigma=3.0, bt=4, sharpen=0.4)),
+    ("float_kalman_bw64", lambda: synth.clip_grays(frames=24, cuts=(12,)), 32,
+     dict(bt=0, bw=64, bh=64, sigma2=1.5, sigma3=2.5, sigma4=3.0)),
+]
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("name,make,bits,params", CASES, ids=[c[0] for c in CASES])
+def test_form_within_tolerance(form, name, make, bits, params):
+    frames = make()
+    got = run(frames, bits, form, **params)
+    ref = oracle.run_clip(frames, bits, threads=16, **params)
+    check(got, ref, tol_for(frames, bits))
+    again = run(frames, bits, form, **params)
+    for a, b in zip(got, again):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_form_spectra_close_to_oracle(form):
+    rng = np.random.default_rng(1)
+    plane = rng.integers(0, 256, (97, 131)).astype(np.uint8)
+    for bw, bh in [(8, 8), (16, 32), (32, 32), (64, 16), (64, 64)]:
+        with F.Engine(131, 97, 8, form=form, bw=bw, bh=bh) as e:
+            e.forward_raw(0, plane)
+            spec = e.spectra(0)
+        pl = oracle.Plane(131, 97, 8, bw=bw, bh=bh)
+        ref = pl.spectra(pl.upload(plane))
+        # spectra scale with the block area (sums of up to bw*bh samples <= 1)
+        assert np.abs(spec - ref).max() <= 2e-6 * bw * bh, (bw, bh)
+
+
+@pytest.mark.parametrize("w,h,bits,params", [
+    (3840, 2160, 10, dict(sigma=3.0, bt=4, sharpen=0.4)),
+    (640, 360, 8, dict(bt=3)),
+    (333, 177, 8, dict(bt=2, bw=16, bh=16, sharpen=0.5)),
+    (97, 61, 8, dict(bt=1, bw=8, bh=8)),
+    (1000, 37, 8, dict(bt=-1, sharpen=0.3)),
+    (41, 700, 8, dict(bt=3, sigma2=1.0, sigma3=3.0, sigma4=4.0)),
+])
+def test_fused_sweep_equals_separate_kernels(w, h, bits, params):
+    # The fused kernel adds each cell's four quadrants in the order of the
+    # separate overlap-add kernel, so the two paths agree bit for bit.
+    if bits == 8:
+        frames = synth.moving_rects(w, h, 5, w + h, lo=16, hi=235, noise=4.0, n_rects=5)
+    else:
+        frames = synth.moving_rects(w, h, 5, w + h, lo=64, hi=940, noise=12.0, dtype=np.uint16, maxval=1023)
+    outs = []
+    for fused in (True, False):
+        flt = F.Filter([[f] for f in frames], F.VideoFormat("gray", bits, 0), form="fast", fused=fused, **params)
+        assert flt.engines[0].info().form == 1
+        outs.append([flt.get_frame(n)[0] for n in range(len(frames))])
+        flt.close()
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
