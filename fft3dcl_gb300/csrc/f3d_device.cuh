@@ -97,16 +97,22 @@ __device__ __forceinline__ void wienner(float& re, float& im, float sx, float sy
 // compiler may move spectra loads freely), kRuntimeBm to read a.bm.
 constexpr int kRuntimeBm = -2;
 
-// Temporal filter + sharpen of bin i (0 <= i < bh*fbw) of block b, with
-// gi = b*bh*fbw + i. Follows src/cpu/reference.cpp:229-409 per bin:
-// degrid correction, bm 2/3/4 temporal DFT + Wiener, bm 1 Wiener, bm 0
-// Kalman (state updated in place), bm -1 pass-through, then sharpen.
-template <int BM>
-__device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, int b, int i, size_t gi) {
+// DC of block b in the current frame's spectrum (the degrid correction's scale).
+__device__ __forceinline__ float block_dc(const InvArgs& a, int b) {
+  return a.dg ? a.s[a.cur][(size_t)b * a.g.bh * a.g.fbw].x : 0.0f;
+}
+
+// Temporal filter + sharpen of bin i (0 <= i < bh*fbw) of a block whose
+// current-frame DC is dc, with gi = b*bh*fbw + i. Follows
+// src/cpu/reference.cpp:229-409 per bin: degrid correction, bm 2/3/4
+// temporal DFT + Wiener, bm 1 Wiener, bm 0 Kalman (state updated in place),
+// bm -1 pass-through, then sharpen. FAST evaluates the 3- and 4-point
+// temporal transforms with fewer additions (a different rounding; the exact
+// form keeps the reference's expressions).
+template <int BM, bool FAST = false>
+__device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i, size_t gi) {
   float d_re = 0.0f, d_im = 0.0f;
   if (a.dg) {
-    const size_t ps = (size_t)a.g.bh * a.g.fbw;
-    const float dc = a.s[a.cur][(size_t)b * ps].x;
     const float2 g = a.gs[i];
     d_re = dc * g.x;
     d_im = dc * g.y;
@@ -160,14 +166,22 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, int b, int i, s
     }
   } else if (bm == 4) {
     const float2 p2 = a.s[0][gi], p1 = a.s[1][gi], c = a.s[2][gi], n = a.s[3][gi];
-    float fp1r = -p2.x + p1.y + c.x - n.y;
-    float fp1i = -p2.y - p1.x + c.y + n.x;
-    float fcr = p2.x + p1.x + c.x + n.x;
-    float fci = p2.y + p1.y + c.y + n.y;
-    float fnr = -p2.x - p1.y + c.x + n.y;
-    float fni = -p2.y + p1.x + c.y - n.x;
-    float fp2r = p2.x - p1.x + c.x - n.x;
-    float fp2i = p2.y - p1.y + c.y - n.y;
+    float fp1r, fp1i, fcr, fci, fnr, fni, fp2r, fp2i;
+    if (FAST) {  // radix 2 x 2: (c +- p2), (p1 +- n)
+      const float sr = c.x + p2.x, si = c.y + p2.y, dr = c.x - p2.x, di = c.y - p2.y;
+      const float tr = p1.x + n.x, ti = p1.y + n.y, er = p1.x - n.x, ei = p1.y - n.y;
+      fcr = sr + tr, fci = si + ti, fp2r = sr - tr, fp2i = si - ti;
+      fp1r = dr + ei, fp1i = di - er, fnr = dr - ei, fni = di + er;
+    } else {
+      fp1r = -p2.x + p1.y + c.x - n.y;
+      fp1i = -p2.y - p1.x + c.y + n.x;
+      fcr = p2.x + p1.x + c.x + n.x;
+      fci = p2.y + p1.y + c.y + n.y;
+      fnr = -p2.x - p1.y + c.x + n.y;
+      fni = -p2.y + p1.x + c.y - n.x;
+      fp2r = p2.x - p1.x + c.x - n.x;
+      fp2i = p2.y - p1.y + c.y - n.y;
+    }
     if (a.dg) {
       fp1r -= 4.0f * d_re;
       fp1i -= 4.0f * d_im;
@@ -254,7 +268,7 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, int b, int i, s
 }
 
 __device__ __forceinline__ float2 filter_bin(const InvArgs& a, int b, int i, size_t gi) {
-  return filter_bin_t<kRuntimeBm>(a, b, i, gi);
+  return filter_bin_t<kRuntimeBm>(a, block_dc(a, b), i, gi);
 }
 
 // One radix-2 DIT stage of length LEN over N register values: butterflies

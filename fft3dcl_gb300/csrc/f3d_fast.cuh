@@ -11,6 +11,14 @@
 
 #include "f3d_device.cuh"
 
+// Unroll factor of the per-bin filter loop (pairs of bins): more bins'
+// loads in flight against more registers.
+#ifndef F3D_FILTER_UNROLL
+#define F3D_FILTER_UNROLL 2
+#endif
+#define F3D_PRAGMA(x) _Pragma(#x)
+#define F3D_UNROLL(n) F3D_PRAGMA(unroll n)
+
 namespace f3d {
 
 // Radix-2 DIT with FMA: twiddles (1,0) and (0,-1) (j = 0 and j = N/4) are
@@ -106,14 +114,15 @@ __device__ __forceinline__ void inverse_block(const InvArgs& a, int b, int t, bo
   // Filter into the tile (two bins per 16-byte store); a partly unrolled loop
   // keeps a few bins' loads in flight without holding the column in registers.
   if (cols) {
-#pragma unroll 2
+    const float dc = block_dc(a, b);
+    F3D_UNROLL(F3D_FILTER_UNROLL)
     for (int r = 0; r < BH; r += 2) {
-      const float2 f0 = filter_bin_t<BM>(a, b, r * C::FBW + t, base + r * C::FBW + t);
-      const float2 f1 = filter_bin_t<BM>(a, b, (r + 1) * C::FBW + t, base + (r + 1) * C::FBW + t);
+      const float2 f0 = filter_bin_t<BM, true>(a, dc, r * C::FBW + t, base + r * C::FBW + t);
+      const float2 f1 = filter_bin_t<BM, true>(a, dc, (r + 1) * C::FBW + t, base + (r + 1) * C::FBW + t);
       tile_pair<C::SB>(S, t, r) = make_float4(f0.x, f0.y, f1.x, f1.y);
     }
     for (int r = t; r < BH; r += C::NY)
-      S[C::NY * C::SB + r] = filter_bin_t<BM>(a, b, r * C::FBW + C::NY, base + r * C::FBW + C::NY);
+      S[C::NY * C::SB + r] = filter_bin_t<BM, true>(a, dc, r * C::FBW + C::NY, base + r * C::FBW + C::NY);
   }
   filtered();
   __syncwarp();
@@ -192,6 +201,94 @@ __device__ __forceinline__ void inverse_block(const InvArgs& a, int b, int t, bo
     }
   }
   __syncwarp();  // S may be reused by the caller from here on
+}
+
+// Square blocks (N = 8, 16, 32): the same filter and inverse with N threads
+// per block (one warp or part of one), so that each thread holds half as
+// much and more warps fit on an SM.
+//   filter   thread t = (c, h), c = t mod N/2, h = t div N/2: column c, rows
+//            h*N/2 .. h*N/2 + N/2 - 1, and Nyquist row t;
+//   columns  the pair (c, 0), (c, 1) inverts column c: the even inputs on
+//            h = 0, the odd ones on h = 1, combined through a shuffle; the
+//            Hermitian parts of columns 0 and N/2 are packed into column 0
+//            first (thread r <= N/2 does rows r and -r);
+//   rows     thread t inverts row t as an N/2-point complex FFT.
+// Tile positions, emit and filtered() are those of inverse_block.
+template <int N, int BM, class Emit, class Filtered>
+__device__ __forceinline__ void inverse_block_sq(const InvArgs& a, int b, int t, bool valid, float2* S,
+                                                 Emit&& emit, Filtered&& filtered) {
+  using C = FCfg<N, N>;
+  constexpr int NY = N / 2, H = N / 2, SB = C::SB, FBW = C::FBW;
+  const size_t base = (size_t)b * C::PS;
+  const int c = t % NY, h = t / NY;
+  if (valid) {
+    const float dc = block_dc(a, b);
+    F3D_UNROLL(F3D_FILTER_UNROLL)
+    for (int k = 0; k < H; k += 2) {
+      const int r = h * H + k;
+      const float2 f0 = filter_bin_t<BM, true>(a, dc, r * FBW + c, base + r * FBW + c);
+      const float2 f1 = filter_bin_t<BM, true>(a, dc, (r + 1) * FBW + c, base + (r + 1) * FBW + c);
+      tile_pair<SB>(S, c, r) = make_float4(f0.x, f0.y, f1.x, f1.y);
+    }
+    S[NY * SB + t] = filter_bin_t<BM, true>(a, dc, t * FBW + NY, base + t * FBW + NY);
+  }
+  filtered();
+  __syncwarp();
+  if (valid && t <= N / 2) {  // Hermitian parts of columns 0 and N/2, packed into column 0
+    const int r = t, m = (N - t) % N;
+    const float2 zr = S[r], zm = S[m];
+    const float2 nr = S[NY * SB + r], nm = S[NY * SB + m];
+    const float ar = 0.5f * (zr.x + zm.x), ai = 0.5f * (zr.y - zm.y);
+    const float qr = 0.5f * (nr.x + nm.x), qi = 0.5f * (nr.y - nm.y);
+    S[r] = make_float2(ar - qi, ai + qr);
+    if (m != r) S[m] = make_float2(ar + qi, qr - ai);
+  }
+  __syncwarp();
+  float2 e[H];
+  if (valid) {
+#pragma unroll
+    for (int j = 0; j < H; j++) e[j] = S[c * SB + 2 * j + h];
+    fft_fast<H, true, 2>(e, a.tw.col);
+    if (h == 1) {
+#pragma unroll
+      for (int y = 0; y < H; y++) {  // e^{+2 pi i y/N} O[y]
+        const float2 w = a.tw.col[y];
+        e[y] = make_float2(fmaf(e[y].x, w.x, e[y].y * w.y), fmaf(e[y].y, w.x, -e[y].x * w.y));
+      }
+    }
+  }
+#pragma unroll
+  for (int y = 0; y < H; y++) {
+    const float ox = __shfl_xor_sync(0xffffffffu, e[y].x, NY);
+    const float oy = __shfl_xor_sync(0xffffffffu, e[y].y, NY);
+    // h = 0: x[y] = E + P at slot 2y; h = 1: x[y + N/2] = E - P at slot 2y+1
+    const float2 x = h == 0 ? make_float2(e[y].x + ox, e[y].y + oy) : make_float2(ox - e[y].x, oy - e[y].y);
+    if (valid) {
+      if (c == 0) {  // real inverses of columns 0 and N/2
+        S[2 * y + h] = make_float2(x.x, 0.0f);
+        S[NY * SB + 2 * y + h] = make_float2(x.y, 0.0f);
+      } else {
+        S[c * SB + 2 * y + h] = x;
+      }
+    }
+  }
+  __syncwarp();
+  if (valid) {
+    const int yp = yperm<N>(t);
+    float2 z2[H];
+#pragma unroll
+    for (int k = 0; k < H; k++) {
+      const float2 yk = S[k * SB + yp], ym = S[(H - k) * SB + yp];
+      const float ax = yk.x + ym.x, ay = yk.y - ym.y;
+      const float bx = yk.x - ym.x, by = yk.y + ym.y;
+      const float2 w = a.tw.row[k];
+      const float px = fmaf(bx, w.x, by * w.y), py = fmaf(by, w.x, -bx * w.y);
+      z2[k] = make_float2(ax - py, ay + px);
+    }
+    fft_fast<H, true, 2>(z2, a.tw.row);
+    emit(t, z2);
+  }
+  __syncwarp();
 }
 
 // Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.

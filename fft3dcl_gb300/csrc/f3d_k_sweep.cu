@@ -10,9 +10,10 @@
 // where q(m,n) is the part of block (m, n)'s windowed inverse over the cell.
 // With half overlap every cell inside the plane has all four blocks.
 //
-// A CTA of 256 threads holds 256/TPB block slots; it owns a strip of
-// TJ = slots-1 cells (slot s computes block column J0+s, the last slot the
-// strip's right neighbour column) and a segment [M0, M1) of block rows. For
+// A CTA of F3D_SWEEP_THREADS threads holds threads/bw block slots (one
+// thread per block row); it owns a strip of TJ = slots-1 cells (slot s
+// computes block column J0+s, the last slot the strip's right neighbour
+// column) and a segment [M0, M1) of block rows. For
 // each block row m it filters and inverts the row's blocks into shared
 // memory, then
 //   - finishes cell row m-1 from the partial sums P (q(m-1,j) + q(m-1,j+1))
@@ -29,12 +30,20 @@
 namespace f3d {
 namespace {
 
-constexpr int kSweepThreads = 256;
+// CTA size and resident CTAs per SM of the sweep (register budget =
+// 65536 / (threads * CTAs)).
+#ifndef F3D_SWEEP_THREADS
+#define F3D_SWEEP_THREADS 256
+#endif
+#ifndef F3D_SWEEP_MINB
+#define F3D_SWEEP_MINB 3
+#endif
+constexpr int kSweepThreads = F3D_SWEEP_THREADS;
 
 template <int BW, int BH>
 struct SCfg {
   using C = FCfg<BW, BH>;
-  static constexpr int TPB = C::TPB;
+  static constexpr int TPB = BW;  // square blocks: inverse_block_sq, one thread per row
   static constexpr int SLOTS = kSweepThreads / TPB;
   static constexpr int TJ = SLOTS - 1;             // cells per strip
   static constexpr int CW = BW / 2, CH = BH / 2;   // cell size
@@ -70,7 +79,7 @@ __device__ __forceinline__ void store4(const SweepArgs& sa, int y, int x, float4
 }
 
 template <int BW, int BH, int BM>
-__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep_fast(const __grid_constant__ SweepArgs sa) {
+__global__ void __launch_bounds__(kSweepThreads, F3D_SWEEP_MINB) k_sweep_fast(const __grid_constant__ SweepArgs sa) {
   using S_ = SCfg<BW, BH>;
   using C = FCfg<BW, BH>;
   constexpr int TPB = S_::TPB, TJ = S_::TJ, CW = S_::CW, CH = S_::CH, QK = S_::QK;
@@ -104,7 +113,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) k_sweep_fast(const __grid_co
     // Windowed rows go back into the tile as sample pairs: (x, x+1) of row y
     // at S[(x/2)*SB + yperm(y)] (see inverse_block).
     const float* win = (n & 1) ? a.win_b : a.win_a;
-    inverse_block<BW, BH, BM>(a, b, t, col_ok, S, [&](int y, const float2(&xy)[BW / 2]) {
+    inverse_block_sq<BW, BM>(a, b, t, col_ok, S, [&](int y, const float2(&xy)[BW / 2]) {
 #pragma unroll
       for (int k = 0; k < BW / 2; k++) {
         const float2 wv = *reinterpret_cast<const float2*>(win + y * BW + 2 * k);
@@ -166,7 +175,7 @@ template <int BW, int BH, int BM>
 cudaError_t launch_bm(const SweepArgs& a, cudaStream_t st) {
   using S_ = SCfg<BW, BH>;
   auto k = k_sweep_fast<BW, BH, BM>;
-  static_assert(S_::SMEM <= 110 * 1024, "two CTAs per SM");
+  static_assert(S_::SMEM * F3D_SWEEP_MINB <= 227 * 1024, "CTAs per SM");
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_::SMEM);
   if (e != cudaSuccess) return e;
   k<<<a.strips * a.segs, kSweepThreads, S_::SMEM, st>>>(a);
@@ -200,12 +209,13 @@ bool sweep_supported(int form, const Geo& g, int bm) {
 }
 
 void sweep_plan(const Geo& g, int sm_count, int* strips, int* segs) {
-  const int tpb = g.bw / 2, tj = kSweepThreads / tpb - 1;
+  const int tpb = g.bw, tj = kSweepThreads / tpb - 1;
   const int cells_x = (g.W + g.bw / 2 - 1) / (g.bw / 2);
   const int cells_y = (g.H + g.bh / 2 - 1) / (g.bh / 2);
   *strips = (cells_x + tj - 1) / tj;
-  // One wave of two CTAs per SM, segments of at least two block rows.
-  int s = (2 * sm_count + *strips - 1) / *strips;
+  // At most one wave of resident CTAs (a partial second wave would double the
+  // time), segments of at least two block rows.
+  int s = F3D_SWEEP_MINB * sm_count / *strips;
   const int maxseg = (cells_y + 1) / 2;
   if (s > maxseg) s = maxseg;
   *segs = s < 1 ? 1 : s;
