@@ -53,6 +53,12 @@ struct f3d_engine {
   f3d_plane_geom geom{};
   Grid grid;
   int device = 0, form = F3D_FORM_EXACT;
+  // Form of the filter/inverse side: the tensor-core form's forward feeds
+  // the fast-form sweep where no tensor-core inverse covers the geometry.
+  int inv_form = F3D_FORM_EXACT;
+  uint8_t* d_tc = nullptr;   // tensor-core form tables
+  size_t tc_bytes = 0;
+  int* d_err = nullptr;      // set by a tensor-core kernel whose wait gave up
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int fbw = 0, ps = 0, bps = 1, fmt = FMT_U8;
@@ -60,6 +66,7 @@ struct f3d_engine {
   size_t spec_bytes = 0;
 
   std::vector<float> win_ana, syn_a, syn_b, pattern, sharpen, gs, tw_row, tw_col;
+  std::vector<double> win_ax, win_ay;  // mode-1 analysis window factors
   float *d_win_ana = nullptr, *d_syn_a = nullptr, *d_syn_b = nullptr;
   float *d_pattern = nullptr, *d_sharpen = nullptr;
   float2* d_gs = nullptr;
@@ -187,7 +194,24 @@ int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int
   a.win = e->d_win_ana;
   a.spec = spec;
   cudaEventRecord(e->ev[0], e->stream);
-  cudaError_t ce = launch_forward(e->form, a, e->stream);
+  cudaError_t ce;
+  if (e->form == F3D_FORM_TC) {
+    TcFwdArgs t{};
+    t.g = a.g;
+    t.src = dsrc;
+    t.pitch = pitch;
+    t.fmt = fmt;
+    t.split = !(fmt == FMT_U8 || (fmt == FMT_U16 && e->geom.bits <= 11));
+    t.norm = e->norm;
+    t.out_scale = t.split ? 1.0f : (fmt == FMT_U8 ? 1.0f / 255.0f : e->norm);
+    t.chroma_norm = e->cnorm;
+    t.tab = e->d_tc;
+    t.spec = spec;
+    t.err = e->d_err;
+    ce = launch_forward_tc(t, e->stream);
+  } else {
+    ce = launch_forward(e->form, a, e->stream);
+  }
   cudaEventRecord(e->ev[1], e->stream);
   e->fwd_timed = true;
   if (ce != cudaSuccess) {
@@ -254,7 +278,7 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
     sa.seam_t = e->d_seam ? e->d_seam + (size_t)(sa.segs - 1) * (a.g.bh / 2) * sa.seam_w : nullptr;
     sa.prefetch = e->sweep_prefetch;
     cudaEventRecord(e->ev[2], e->stream);
-    cudaError_t ce = launch_sweep(e->form, sa, e->stream);
+    cudaError_t ce = launch_sweep(e->inv_form, sa, e->stream);
     cudaEventRecord(e->ev[4], e->stream);
     cudaEventRecord(e->ev[3], e->stream);
     e->proc_timed = true;
@@ -262,7 +286,7 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
     return F3D_OK;
   }
   cudaEventRecord(e->ev[2], e->stream);
-  cudaError_t ce = launch_filter_inverse(e->form, a, e->stream);
+  cudaError_t ce = launch_filter_inverse(e->inv_form, a, e->stream);
   cudaEventRecord(e->ev[4], e->stream);
   if (ce != cudaSuccess) return e->cuda_fail(ce, "the filter/inverse launch");
   if (a.kalman_init) e->kalman_first = false;
@@ -344,7 +368,9 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
   // Kalman's reset is a threshold on per-bin frame differences: any rounding
   // difference flips bins near it, so bt=0 runs the exact kernels in every
   // form. Blocks the faster forms do not cover (4-wide) use them too.
-  if (ip.bm == 0 || !form_supported(form, ip.bw, ip.bh)) form = F3D_FORM_EXACT;
+  if (ip.bm == 0) form = F3D_FORM_EXACT;
+  if (form == F3D_FORM_TC && !tc_supported(ip.mode, ip.bw, ip.bh, ip.bm)) form = F3D_FORM_FAST;
+  if (!form_supported(form, ip.bw, ip.bh)) form = F3D_FORM_EXACT;
   if (!form_supported(form, ip.bw, ip.bh))
     return fail_thread(F3D_E_UNSUPPORTED,
                        "FFT3DCL: block size " + std::to_string(ip.bw) + "x" + std::to_string(ip.bh) +
@@ -367,6 +393,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
   e->grid = make_grid(ip);
   e->device = device;
   e->form = form;
+  e->inv_form = form == F3D_FORM_TC ? F3D_FORM_FAST : form;
   e->fbw = ip.bw / 2 + 1;
   e->ps = e->fbw * ip.bh;
   e->spec_bytes = sizeof(float2) * (size_t)e->grid.nb * e->ps;
@@ -395,6 +422,10 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
     e->pattern = std::move(t.pattern);
     e->sharpen = std::move(t.sharpen);
     e->gs = std::move(t.gs);
+    if (ip.mode == 1) {
+      std::vector<float> a, sa, sb;
+      windows_mode1(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, a, sa, sb, &e->win_ax, &e->win_ay);
+    }
   }
 
   auto finish_fail = [&](int code) {
@@ -428,6 +459,15 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
       (ce = up(&e->d_sharpen, e->sharpen)) != cudaSuccess ||
       (ce = up(reinterpret_cast<float**>(&e->d_gs), e->gs)) != cudaSuccess)
     return finish_fail(e->cuda_fail(ce, "table upload"));
+  if (form == F3D_FORM_TC) {
+    const std::vector<uint8_t> tab = tc_tables(ip.bw, e->win_ax, e->win_ay, e->syn_a, e->syn_b);
+    if (tab.empty()) return finish_fail(e->fail(F3D_E_UNSUPPORTED, "FFT3DCL: no tensor-core tables for this block size"));
+    e->tc_bytes = tab.size();
+    if ((ce = e->alloc(&e->d_tc, e->tc_bytes)) != cudaSuccess ||
+        (ce = cudaMemcpy(e->d_tc, tab.data(), tab.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (ce = e->alloc(&e->d_err, sizeof(int))) != cudaSuccess || (ce = cudaMemset(e->d_err, 0, sizeof(int))) != cudaSuccess)
+      return finish_fail(e->cuda_fail(ce, "tensor-core table upload"));
+  }
   if ((ce = e->alloc(&e->d_in, plane_bytes)) != cudaSuccess ||
       (ce = e->alloc(&e->d_out, plane_bytes)) != cudaSuccess ||
       (ce = e->alloc(&e->d_blocks, sizeof(float) * bwbh * e->grid.nb)) != cudaSuccess)
@@ -440,7 +480,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
       return finish_fail(e->cuda_fail(ce, "Kalman state allocation"));
   }
   const Geo geo = make_geo(e);
-  if (!(opts && (opts->flags & F3D_FLAG_UNFUSED)) && sweep_supported(form, geo, ip.bm)) {
+  if (!(opts && (opts->flags & F3D_FLAG_UNFUSED)) && sweep_supported(e->inv_form, geo, ip.bm)) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     sweep_plan(geo, sms > 0 ? sms : 1, &e->sweep_strips, &e->sweep_segs);
@@ -465,6 +505,8 @@ void f3d_engine_destroy(f3d_engine* e) {
     for (float2*& m : e->pool) e->release(m, e->spec_bytes);
     e->pool.clear();
     e->release(e->d_win_ana, e->win_ana.size() * sizeof(float));
+    e->release(e->d_tc, e->tc_bytes);
+    e->release(e->d_err, sizeof(int));
     e->release(e->d_syn_a, e->syn_a.size() * sizeof(float));
     e->release(e->d_syn_b, e->syn_b.size() * sizeof(float));
     e->release(e->d_pattern, e->pattern.size() * sizeof(float));
@@ -635,6 +677,12 @@ int f3d_synchronize(f3d_engine* e) {
   Lock l(e);
   cudaError_t ce = cudaStreamSynchronize(e->stream);
   if (ce != cudaSuccess) return e->cuda_fail(ce, "synchronize");
+  if (e->d_err) {
+    int flag = 0;
+    ce = cudaMemcpy(&flag, e->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "synchronize");
+    if (flag) return e->fail(F3D_E_CUDA, "FFT3DCL: a tensor-core wait timed out; results since the last check are invalid");
+  }
   return F3D_OK;
 }
 

@@ -175,8 +175,11 @@ inline std::vector<float> window_mode0(int bw, int bh) {
 
 // buildWindowsMode1, src/cpu/tables.cpp:21-105, plus the odd-parity synthesis
 // window shifted by (bw-ow), src/cpu/reference.cpp:51-57.
+// The analysis window is separable: A[y][x] = float(ax[x] * ay[y]); ax and
+// ay (double) are returned when asked for.
 inline void windows_mode1(int bw, int bh, int ow, int oh, int wintype, std::vector<float>& A,
-                          std::vector<float>& synA, std::vector<float>& synB) {
+                          std::vector<float>& synA, std::vector<float>& synB,
+                          std::vector<double>* ax = nullptr, std::vector<double>* ay = nullptr) {
   std::vector<double> wanx(ow), wany(oh), wsynx(ow), wsyny(oh);
   auto half_cos = [](int i, int o) { return std::cos(kPi * (i - o + 0.5) / (o * 2.0)); };
   for (int i = 0; i < ow; i++) {
@@ -233,6 +236,8 @@ inline void windows_mode1(int bw, int bh, int ow, int oh, int wintype, std::vect
       wySA[ly] = wsyny[bh - 1 - ly];
     }
   }
+  if (ax) *ax = wxA;
+  if (ay) *ay = wyA;
   A.assign(bw * bh, 0.0f);
   synA.assign(bw * bh, 0.0f);
   std::vector<float> sb(bw * bh);

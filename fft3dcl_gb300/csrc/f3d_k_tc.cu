@@ -1,0 +1,494 @@
+// f3d_k_tc.cu -- the tensor-core form: 2D block DFTs as dense DFT-matrix
+// products on the fifth-generation tensor cores (tcgen05), fp16 operands
+// split into hi + lo parts with fp32 accumulation in tensor memory.
+//
+// Forward transform of an n x n real block X (n = 32) with separable
+// analysis window wx[x] * wy[y] (src/cpu/tables.cpp:21-105), folded into the
+// DFT matrices:
+//   step 1 (rows):    Z[y][j] = sum_x X[y][x] * B1[j][x], the n real outputs
+//                     j = (Re Z0, Re Z(n/2), Re Z1, Im Z1, .., Im Z(n/2-1)) of
+//                     each row's real DFT;
+//   step 2 (columns): for each packed column k' = 0..n/2-1 (k' = 0 carries
+//                     Z0 + i Z(n/2)), Y[ky][k'] = sum_y e^(-2 pi i ky y/n)
+//                     wy[y] Z[y][k'] as a real 2n x 2n matrix B2 acting on
+//                     interleaved (re, im) pairs;
+//   unpacking:        Y0 = (P + conj P(-ky))/2, Y(n/2) = (P - conj P(-ky))/2i
+//                     for the packed column P.
+// This equals fft2dRealForward of the windowed block (src/cpu/fft.cpp:68-86,
+// src/cpu/reference.cpp:140-170) up to fp32 rounding. The chroma offset is
+// removed in the spectrum (c * DFT(window)), the sample scale (1/255,
+// 2^(16-bits)/65535) applied to the output.
+//
+// Tiling: a group of G = 8 blocks; step 1 runs as two M = 128 tiles (rows =
+// 4 blocks x 32 rows, N = 32, K = 32), step 2 as one M = 128 tile (rows = 8
+// blocks x 16 packed columns, N = 64, K = 64). Operands hi/lo: step 1 uses
+// X exactly (integer samples of up to 11 bits are exact in fp16) times
+// B1hi + B1lo, or Xhi*B1hi + Xhi*B1lo + Xlo*B1hi; step 2 Ahi*Bhi + Ahi*Blo +
+// Alo*Bhi. The spectra of a group (8 x 4352 bytes, contiguous in HBM) leave
+// shared memory by one bulk copy.
+#include "f3d_device.cuh"
+#include "f3d_tc.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace f3d {
+namespace {
+
+constexpr double kPiD = 3.14159265358979323846;
+
+// Byte offsets of the table sections for n x n blocks.
+template <int N>
+struct TcTab {
+  static constexpr int FBW = N / 2 + 1;
+  static constexpr uint32_t B1HI = 0, B1LO = B1HI + N * N * 2;
+  static constexpr uint32_t B2HI = B1LO + N * N * 2, B2LO = B2HI + 8 * N * N;
+  static constexpr uint32_t WSPEC = B2LO + 8 * N * N;  // float2 [N][FBW]
+  static constexpr uint32_t C2HI = WSPEC + N * FBW * 8, C2LO = C2HI + 8 * N * N;
+  static constexpr uint32_t C1HI = C2LO + 8 * N * N, C1LO = C1HI + N * N * 2;
+  static constexpr uint32_t SYNA = C1LO + N * N * 2, SYNB = SYNA + N * N * 4;  // float [N][N]
+  static constexpr uint32_t TOTAL = SYNB + N * N * 4;
+  static_assert(WSPEC % 16 == 0 && C2HI % 16 == 0 && SYNA % 16 == 0, "16-byte sections");
+};
+
+// Scale of the filtered spectrum before its hi/lo split in the inverse,
+// undone in the synthesis window: keeps the column sums inside fp16 range.
+constexpr float kInvPre = 1.0f / 16.0f;
+
+// Kernel configuration for n x n blocks.
+template <int N>
+struct TcCfg {
+  static constexpr int NY = N / 2, FBW = NY + 1, PS = N * FBW;
+  static constexpr int G = 128 / NY;       // blocks per group (step-2 tile rows: G x NY)
+  static constexpr int BPT1 = 128 / N;     // blocks per step-1 tile (rows: BPT1 x N)
+  static constexpr int T1 = G / BPT1;      // step-1 tiles per group
+  static constexpr int K1 = N, N1 = N;     // step 1: K = x, N = packed outputs
+  static constexpr int K2 = 2 * N, N2 = 2 * N;
+  static constexpr uint32_t A1_BYTES = 128 * K1 * 2, A2_BYTES = 128 * K2 * 2;
+  static constexpr uint32_t B1_BYTES = N1 * K1 * 2, B2_BYTES = N2 * K2 * 2;
+  static constexpr uint32_t TMEM_COLS = 128;
+  static constexpr uint32_t D1_COL = 0, D2_COL = 64;
+  static_assert(N == 32, "the tensor-core form is built for 32 x 32 blocks");
+  static_assert(T1 * N1 <= (int)D2_COL && D2_COL + N2 <= (int)TMEM_COLS, "tensor memory columns");
+};
+
+constexpr int kTcThreads = 256;
+constexpr uint64_t kWaitNs = 1000000000ull;  // one second
+
+// ---- forward ---------------------------------------------------------------
+
+// Shared memory of the forward kernel (offsets from a 1024-aligned base).
+template <int N>
+struct FwdSmem {
+  using C = TcCfg<N>;
+  static constexpr uint32_t B2 = 0;                       // hi, lo
+  static constexpr uint32_t B1 = B2 + 2 * C::B2_BYTES;    // hi, lo
+  static constexpr uint32_t A2 = (B1 + 2 * C::B1_BYTES + 1023) / 1024 * 1024;  // hi, lo (SWIZZLE_128B)
+  static constexpr uint32_t A1 = A2 + 2 * C::A2_BYTES;    // [tile][hi, lo]
+  static constexpr uint32_t STAGE = A2;                   // spectra of the group, after step 2
+  static constexpr uint32_t BAR = A1 + 2 * C::T1 * C::A1_BYTES;
+  static constexpr uint32_t TSLOT = BAR + 16;
+  static constexpr uint32_t BYTES = TSLOT + 16 + 1024;    // + alignment slack
+  static_assert(STAGE + C::G * C::PS * 8 <= BAR, "staging fits the operand space");
+};
+
+// Gather of a group's samples: task q covers 16 source bytes (16/BPS samples)
+// of row y of block bl. The raw bytes are fetched into registers one group
+// ahead, so that their loads are in flight while the tensor cores work on the
+// current group, and deposited into the step-1 operand as fp16.
+template <int N, int BPS>
+struct Gather {
+  static constexpr int S = 16 / BPS;                   // samples per task
+  static constexpr int TPR = N / S;                    // tasks per block row
+  static constexpr int TASKS = TcCfg<N>::G * N * TPR;
+  static constexpr int TPT = TASKS / kTcThreads;       // tasks per thread
+  static_assert(TASKS % kTcThreads == 0 && S >= 4, "task split");
+};
+
+template <int N, int BPS>
+__device__ __forceinline__ void fetch(const TcFwdArgs& a, int b0, int nvalid, uint4 (&r)[Gather<N, BPS>::TPT]) {
+  using Gt = Gather<N, BPS>;
+#pragma unroll
+  for (int i = 0; i < Gt::TPT; i++) {
+    const int q = threadIdx.x + i * kTcThreads;
+    const int c = q % Gt::TPR, ry = q / Gt::TPR;
+    const int bl = ry / N, y = ry - bl * N;
+    r[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (bl >= nvalid) continue;
+    int bx, by, par;
+    block_origin(a.g, b0 + bl, bx, by, par);
+    if (bx >= 0 && by >= 0 && bx + N <= a.g.W && by + N <= a.g.H) {
+      const uint8_t* p = a.src + (long long)(by + y) * a.pitch + (long long)bx * BPS + 16 * c;
+      if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+        r[i] = __ldg(reinterpret_cast<const uint4*>(p));
+        continue;
+      }
+    }
+    // Mirrored or unaligned: one sample at a time (src/cpu/reference.cpp:10-17).
+    const uint8_t* row = a.src + (long long)mirror_i(by + y, a.g.H) * a.pitch;
+    uint32_t w[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int k = 0; k < Gt::S; k++) {
+      const int x = mirror_i(bx + c * Gt::S + k, a.g.W);
+      uint32_t v;
+      if (BPS == 1) v = row[x];
+      else if (BPS == 2) v = reinterpret_cast<const uint16_t*>(row)[x];
+      else v = reinterpret_cast<const uint32_t*>(row)[x];
+      w[(k * BPS) / 4] |= v << (8 * ((k * BPS) % 4));
+    }
+    r[i] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// Raw bytes -> fp16 (hi, and lo on the split path) in A1[tile][part]: rows
+// (block % BPT1, y), K = x.
+template <int N, int BPS>
+__device__ __forceinline__ void deposit(const TcFwdArgs& a, uint8_t* a1, const uint4 (&r)[Gather<N, BPS>::TPT]) {
+  using Gt = Gather<N, BPS>;
+  using C = TcCfg<N>;
+#pragma unroll
+  for (int i = 0; i < Gt::TPT; i++) {
+    const int q = threadIdx.x + i * kTcThreads;
+    const int c = q % Gt::TPR, ry = q / Gt::TPR;
+    const int bl = ry / N, y = ry - bl * N;
+    const int tile = bl / C::BPT1, row = (bl % C::BPT1) * N + y;
+    const uint32_t w[4] = {r[i].x, r[i].y, r[i].z, r[i].w};
+    float v[Gt::S];
+#pragma unroll
+    for (int k = 0; k < Gt::S; k++) {
+      if (BPS == 1) v[k] = (float)((w[k >> 2] >> (8 * (k & 3))) & 0xffu);
+      else if (BPS == 2) v[k] = (float)((w[k >> 1] >> (16 * (k & 1))) & 0xffffu) * (a.split ? a.norm : 1.0f);
+      else v[k] = __uint_as_float(w[k]);
+    }
+    uint32_t h[Gt::S / 2], l[Gt::S / 2];
+#pragma unroll
+    for (int k = 0; k < Gt::S / 2; k++) tc::split_pair(v[2 * k], v[2 * k + 1], h[k], l[k]);
+    uint8_t* t0 = a1 + tile * 2 * C::A1_BYTES;
+    const int x0 = c * Gt::S;
+    if (Gt::S >= 8) {
+#pragma unroll
+      for (int j = 0; j < Gt::S / 8; j++) {
+        const uint32_t o = tc::off_il(row, x0 + 8 * j, C::K1);
+        *reinterpret_cast<uint4*>(t0 + o) = make_uint4(h[4 * j], h[4 * j + 1], h[4 * j + 2], h[4 * j + 3]);
+        if (a.split)
+          *reinterpret_cast<uint4*>(t0 + C::A1_BYTES + o) = make_uint4(l[4 * j], l[4 * j + 1], l[4 * j + 2], l[4 * j + 3]);
+      }
+    } else {
+      const uint32_t o = tc::off_il(row, x0, C::K1);
+      *reinterpret_cast<uint2*>(t0 + o) = make_uint2(h[0], h[1]);
+      if (a.split) *reinterpret_cast<uint2*>(t0 + C::A1_BYTES + o) = make_uint2(l[0], l[1]);
+    }
+  }
+}
+
+template <int N, int BPS>
+__global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_constant__ TcFwdArgs a) {
+  using C = TcCfg<N>;
+  using L = FwdSmem<N>;
+  using T = TcTab<N>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = tc::smem_u32(sm);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L::BAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + L::TSLOT);
+  float2* stage = reinterpret_cast<float2*>(sm + L::STAGE);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // Constant operands: B2 (hi, lo) and B1 (hi, lo) are contiguous in the table.
+  {
+    const uint4* src2 = reinterpret_cast<const uint4*>(a.tab + T::B2HI);
+    uint4* dst2 = reinterpret_cast<uint4*>(sm + L::B2);
+    for (int i = tid; i < (int)(2 * C::B2_BYTES / 16); i += kTcThreads) dst2[i] = src2[i];
+    const uint4* src1 = reinterpret_cast<const uint4*>(a.tab + T::B1HI);
+    uint4* dst1 = reinterpret_cast<uint4*>(sm + L::B1);
+    for (int i = tid; i < (int)(2 * C::B1_BYTES / 16); i += kTcThreads) dst1[i] = src1[i];
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, C::TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&bar[0], 1);
+    tc::mbar_init(&bar[1], 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const int ngroups = (a.g.nb + C::G - 1) / C::G;
+  uint32_t phase = 0;
+  uint4 raw[Gather<N, BPS>::TPT];
+  if ((int)blockIdx.x < ngroups) fetch<N, BPS>(a, blockIdx.x * C::G, min(C::G, a.g.nb - (int)blockIdx.x * C::G), raw);
+
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int b0 = grp * C::G;
+    const int nvalid = min(C::G, a.g.nb - b0);
+    // The previous group's bulk store must have read the staging area, which
+    // aliases the operands written next.
+    if (tid == 0) tc::bulk_wait_read();
+    __syncthreads();
+
+    // 1. This group's samples into A1; the next group's loads start.
+    deposit<N, BPS>(a, sm + L::A1, raw);
+    const int nxt = grp + gridDim.x;
+    if (nxt < ngroups) fetch<N, BPS>(a, nxt * C::G, min(C::G, a.g.nb - nxt * C::G), raw);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+
+    // 2. Step 1 on the tensor cores: D1[tile] = A1 * B1^T (two or three passes).
+    if (tid == 0) {
+      tc::fence_after_sync();
+      constexpr uint32_t id1 = tc::idesc_f16(128, C::N1);
+      const uint32_t sbo = (C::K1 / 8) * 128;
+      for (int t = 0; t < C::T1; t++) {
+        const uint32_t a_hi = sbase + L::A1 + t * 2 * C::A1_BYTES, a_lo = a_hi + C::A1_BYTES;
+        const uint32_t d = tmem + C::D1_COL + t * C::N1;
+        for (int ks = 0; ks < C::K1 / 16; ks++) {
+          const uint64_t ah = tc::sdesc(a_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+          const uint64_t bh = tc::sdesc(sbase + L::B1 + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+          const uint64_t bl = tc::sdesc(sbase + L::B1 + C::B1_BYTES + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+          tc::mma_f16(d, ah, bh, id1, ks > 0);
+          tc::mma_f16(d, ah, bl, id1, 1);
+          if (a.split) tc::mma_f16(d, tc::sdesc(a_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE), bh, id1, 1);
+        }
+      }
+      tc::mma_commit(&bar[0]);
+    }
+    // Every thread takes the same branch: a wait that gave up anywhere ends
+    // the sweep of groups for the whole CTA.
+    if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
+      if (tid == 0) atomicOr(a.err, 1);
+      break;
+    }
+    tc::fence_after_sync();
+
+    // 3. D1 -> A2 (hi, lo): row (block, k'), K = 2y + (re, im).
+    {
+      const int t = warp >> 2, s = warp & 3;
+      const int r1 = 32 * s + lane;
+      const int bl = t * C::BPT1 + r1 / N, y = r1 % N;
+      float v[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
+#pragma unroll
+      for (int kp = 0; kp < C::NY; kp++) {
+        uint32_t hi, lo;
+        tc::split_pair(v[2 * kp], v[2 * kp + 1], hi, lo);
+        const uint32_t o = tc::off_sw128(bl * C::NY + kp, 2 * y);
+        *reinterpret_cast<uint32_t*>(sm + L::A2 + o) = hi;
+        *reinterpret_cast<uint32_t*>(sm + L::A2 + C::A2_BYTES + o) = lo;
+      }
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+
+    // 4. Step 2: D2 = A2 * B2^T, three passes.
+    if (tid == 0) {
+      tc::fence_after_sync();
+      constexpr uint32_t id2 = tc::idesc_f16(128, C::N2);
+      const uint32_t sbo_b = (C::K2 / 8) * 128;
+      const uint32_t d = tmem + C::D2_COL;
+      for (int ks = 0; ks < C::K2 / 16; ks++) {
+        const uint64_t ah = tc::sdesc(sbase + L::A2 + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+        const uint64_t al = tc::sdesc(sbase + L::A2 + C::A2_BYTES + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+        const uint64_t bh = tc::sdesc(sbase + L::B2 + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
+        const uint64_t bl = tc::sdesc(sbase + L::B2 + C::B2_BYTES + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
+        tc::mma_f16(d, ah, bh, id2, ks > 0);
+        tc::mma_f16(d, ah, bl, id2, 1);
+        tc::mma_f16(d, al, bh, id2, 1);
+      }
+      tc::mma_commit(&bar[1]);
+    }
+    if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
+      if (tid == 0) atomicOr(a.err, 1);
+      break;
+    }
+    phase ^= 1;
+    tc::fence_after_sync();
+
+    // 5. D2 -> staging [block][ky][kx], scaled; column 0 holds the packed P.
+    {
+      const int s = warp & 3, h = warp >> 2;
+      const int r2 = 32 * s + lane;
+      const int bl = r2 / C::NY, kp = r2 % C::NY;
+      float v[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + 32 * h, v);
+      float2* o = stage + bl * C::PS + kp;
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const int ky = 16 * h + j;
+        o[ky * C::FBW] = make_float2(v[2 * j] * a.out_scale, v[2 * j + 1] * a.out_scale);
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+
+    // 6. Unpack columns 0 and n/2; chroma offset.
+    for (int q = tid; q < C::G * N; q += kTcThreads) {
+      const int bl = q / N, ky = q % N;
+      float2* blk = stage + bl * C::PS;
+      const float2 P = blk[ky * C::FBW], Q = blk[((N - ky) % N) * C::FBW];
+      __syncwarp();
+      // Both halves of a pair (ky, n-ky) sit in the same warp for N = 32.
+      blk[ky * C::FBW] = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
+      blk[ky * C::FBW + C::NY] = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
+      if (a.chroma_norm != 0.0f) {
+        const float2* ws = reinterpret_cast<const float2*>(a.tab + T::WSPEC) + ky * C::FBW;
+        for (int kx = 0; kx < C::FBW; kx++) {
+          const float2 w = ws[kx];
+          float2& z = blk[ky * C::FBW + kx];
+          z.x -= a.chroma_norm * w.x;
+          z.y -= a.chroma_norm * w.y;
+        }
+      }
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+
+    // 7. One bulk copy of the group's spectra to HBM.
+    if (tid == 0 && nvalid > 0) {
+      tc::bulk_store(a.spec + (size_t)b0 * C::PS, stage, (uint32_t)(nvalid * C::PS * 8));
+      tc::bulk_commit();
+    }
+  }
+  if (tid == 0) tc::bulk_wait();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
+}
+
+template <class K>
+cudaError_t prepare(K k, size_t smem) {
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+// Host-side fp16 hi/lo split of a double.
+void split_h(double v, __half& hi, __half& lo) {
+  hi = __float2half_rn((float)v);
+  lo = __float2half_rn((float)(v - (double)__half2float(hi)));
+}
+void put_pair(std::vector<uint8_t>& t, uint32_t hi_base, uint32_t lo_base, uint32_t off, double v) {
+  __half h, l;
+  split_h(v, h, l);
+  std::memcpy(t.data() + hi_base + off, &h, 2);
+  std::memcpy(t.data() + lo_base + off, &l, 2);
+}
+
+template <int N>
+std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<double>& wy,
+                              const std::vector<float>& syn_a, const std::vector<float>& syn_b) {
+  using T = TcTab<N>;
+  constexpr int NY = N / 2, FBW = NY + 1;
+  std::vector<uint8_t> t(T::TOTAL, 0);
+  auto cs = [](int k, int x, double& c, double& s) {
+    const double th = 2.0 * kPiD * (double)((k * x) % N) / N;
+    c = std::cos(th);
+    s = std::sin(th);
+  };
+  // B1 [j][x]: packed real row DFT with wx folded in.
+  for (int j = 0; j < N; j++)
+    for (int x = 0; x < N; x++) {
+      double v;
+      if (j == 0) v = 1.0;
+      else if (j == 1) v = (x & 1) ? -1.0 : 1.0;
+      else {
+        double c, s;
+        cs(j / 2, x, c, s);
+        v = (j & 1) ? -s : c;
+      }
+      put_pair(t, T::B1HI, T::B1LO, tc::off_il(j, x, N), v * wx[x]);
+    }
+  // B2 [2ky+ro][2y+ri]: complex column DFT with wy folded in.
+  for (int ky = 0; ky < N; ky++)
+    for (int y = 0; y < N; y++) {
+      double c, s;
+      cs(ky, y, c, s);
+      const double w = wy[y];
+      put_pair(t, T::B2HI, T::B2LO, tc::off_il(2 * ky, 2 * y, 2 * N), w * c);
+      put_pair(t, T::B2HI, T::B2LO, tc::off_il(2 * ky, 2 * y + 1, 2 * N), w * s);
+      put_pair(t, T::B2HI, T::B2LO, tc::off_il(2 * ky + 1, 2 * y, 2 * N), -w * s);
+      put_pair(t, T::B2HI, T::B2LO, tc::off_il(2 * ky + 1, 2 * y + 1, 2 * N), w * c);
+    }
+  // Spectrum of the analysis window (the chroma offset's contribution).
+  for (int ky = 0; ky < N; ky++)
+    for (int kx = 0; kx < FBW; kx++) {
+      double re = 0.0, im = 0.0;
+      for (int y = 0; y < N; y++)
+        for (int x = 0; x < N; x++) {
+          const double th = 2.0 * kPiD * (double)((ky * y + kx * x) % N) / N;
+          re += wy[y] * wx[x] * std::cos(th);
+          im -= wy[y] * wx[x] * std::sin(th);
+        }
+      const float f[2] = {(float)re, (float)im};
+      std::memcpy(t.data() + T::WSPEC + (ky * FBW + kx) * 8, f, 8);
+    }
+  // C2 [2y+ro][2ky+ri]: complex column inverse DFT (unnormalised).
+  for (int y = 0; y < N; y++)
+    for (int ky = 0; ky < N; ky++) {
+      double c, s;
+      cs(ky, y, c, s);
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y, 2 * ky, 2 * N), c);
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y, 2 * ky + 1, 2 * N), -s);
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y + 1, 2 * ky, 2 * N), s);
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y + 1, 2 * ky + 1, 2 * N), c);
+    }
+  // C1 [x][j]: real row inverse from the packed half spectrum.
+  for (int x = 0; x < N; x++)
+    for (int j = 0; j < N; j++) {
+      double v;
+      if (j == 0) v = 1.0;
+      else if (j == 1) v = (x & 1) ? -1.0 : 1.0;
+      else {
+        double c, s;
+        cs(j / 2, x, c, s);
+        v = (j & 1) ? -2.0 * s : 2.0 * c;
+      }
+      put_pair(t, T::C1HI, T::C1LO, tc::off_il(x, j, N), v);
+    }
+  // Synthesis windows with the inverse's 1/n^2 and the pre-scale undone.
+  const float k = 1.0f / (kInvPre * N * N);
+  for (int i = 0; i < N * N; i++) {
+    const float fa = syn_a.empty() ? 0.0f : syn_a[i] * k, fb = syn_b.empty() ? 0.0f : syn_b[i] * k;
+    std::memcpy(t.data() + T::SYNA + i * 4, &fa, 4);
+    std::memcpy(t.data() + T::SYNB + i * 4, &fb, 4);
+  }
+  return t;
+}
+
+}  // namespace
+
+bool tc_supported(int mode, int bw, int bh, int bm) { return mode == 1 && bw == 32 && bh == 32 && bm != 0; }
+
+std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::vector<double>& wy,
+                               const std::vector<float>& syn_a, const std::vector<float>& syn_b) {
+  if (n == 32 && (int)wx.size() == n && (int)wy.size() == n) return tables_n<32>(wx, wy, syn_a, syn_b);
+  return {};
+}
+
+cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st) {
+  if (a.g.bw != 32 || a.g.bh != 32 || a.g.mode != 1) return cudaErrorNotSupported;
+  using C = TcCfg<32>;
+  constexpr size_t smem = FwdSmem<32>::BYTES;
+  auto k = a.fmt == FMT_U8 ? k_forward_tc<32, 1> : a.fmt == FMT_U16 ? k_forward_tc<32, 2> : k_forward_tc<32, 4>;
+  cudaError_t attr = prepare(k, smem);
+  if (attr != cudaSuccess) return attr;
+  const int ngroups = (a.g.nb + C::G - 1) / C::G;
+  if (ngroups == 0) return cudaSuccess;
+  const int grid = std::min(ngroups, 2 * sm_count());
+  k<<<grid, kTcThreads, smem, st>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace f3d

@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 
 namespace f3d {
 
@@ -117,9 +118,33 @@ F3D_DECLARE_EXACT(32)
 F3D_DECLARE_EXACT(64)
 #undef F3D_DECLARE_EXACT
 
-// Fast-form launchers (f3d_k_fast.cu); spectra are column-major per block.
+// Fast-form launchers (f3d_k_fast.cu).
 cudaError_t launch_forward_fast(const FwdArgs& a, cudaStream_t st);
 cudaError_t launch_inverse_fast(const InvArgs& a, cudaStream_t st);
+
+// Tensor-core form (f3d_k_tc.cu): block transforms as DFT-matrix products on
+// the tensor cores, fp16 operands split into hi + lo parts, fp32
+// accumulation in tensor memory. Mode 1, square 32x32 blocks.
+struct TcFwdArgs {
+  Geo g;
+  const uint8_t* src;  // plane in device memory
+  long long pitch;
+  int fmt;
+  int split;           // 0: integer samples enter as fp16 exactly (8..11 bits); 1: hi + lo parts
+  float norm;          // 16-bit normalisation (split path)
+  float out_scale;     // applied to the spectra: 1/255 or norm on the integer path, 1 on the split path
+  float chroma_norm;
+  const uint8_t* tab;  // device copy of tc_tables()
+  float2* spec;        // out: nb x bh x fbw half spectra
+  int* err;            // set non-zero when a tensor-core wait gives up
+};
+bool tc_supported(int mode, int bw, int bh, int bm);
+// DFT matrices (fp16 hi/lo, in the kernels' shared-memory operand layout),
+// the analysis window's spectrum and the scaled synthesis windows, for
+// n x n blocks whose mode-1 analysis window is wx[x] * wy[y].
+std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::vector<double>& wy,
+                               const std::vector<float>& syn_a, const std::vector<float>& syn_b);
+cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st);
 
 // Counts one kernel launch made by this library (all engines, all threads).
 void count_launch();

@@ -13,7 +13,7 @@ from fft3dcl_gb300 import synth
 
 pytestmark = pytest.mark.gpu
 
-FORMS = ["fast"]
+FORMS = ["fast", "tc"]
 
 
 def tol_for(frames, bits):
@@ -46,6 +46,9 @@ CASES = [
     ("gray8_bw8x64_overlap", lambda: synth.clip_gray8(frames=5), 8, dict(bw=8, bh=64, ow=2, oh=16)),
     ("gray8_mode0", lambda: synth.clip_gray8(frames=5), 8, dict(mode=0, bw=16, bh=32)),
     ("p10_4k_bt4", lambda: synth.clip_yuv420p10_luma(frames=5), 10, dict(sigma=3.0, bt=4, sharpen=0.4)),
+    ("float_bt3", lambda: synth.clip_grays(frames=5), 32, dict(bt=3, sharpen=0.3)),
+    ("p12_bt2", lambda: synth.moving_rects(160, 96, 4, 7, lo=256, hi=3800, noise=20.0, dtype=np.uint16,
+                                           maxval=4095), 12, dict(bt=2)),
     ("float_kalman_bw64", lambda: synth.clip_grays(frames=24, cuts=(12,)), 32,
      dict(bt=0, bw=64, bh=64, sigma2=1.5, sigma3=2.5, sigma4=3.0)),
 ]
@@ -100,3 +103,16 @@ def test_fused_sweep_equals_separate_kernels(w, h, bits, params):
         flt.close()
     for a, b in zip(*outs):
         np.testing.assert_array_equal(a, b)
+
+
+from test_parity_gpu import CASES as GOLDEN_CASES, gpu_clip, load_case  # noqa: E402
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("path", GOLDEN_CASES, ids=[p.rsplit("/", 1)[-1][:-4] for p in GOLDEN_CASES])
+def test_form_golden_within_tolerance(form, path):
+    # The golden outputs come from the reference's CPU backend; chroma planes,
+    # 16-bit and float samples and every temporal mode are among them.
+    frames, out, bits, chroma, params = load_case(path)
+    got = gpu_clip(frames, bits, chroma=chroma, form=form, **params)
+    check(got, out, tol_for(frames, bits))
