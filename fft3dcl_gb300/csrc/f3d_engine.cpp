@@ -66,7 +66,7 @@ struct f3d_engine {
   size_t spec_bytes = 0;
 
   std::vector<float> win_ana, syn_a, syn_b, pattern, sharpen, gs, tw_row, tw_col;
-  std::vector<double> win_ax, win_ay;  // mode-1 analysis window factors
+  Mode1Axes axes;  // mode-1 window factors
   float *d_win_ana = nullptr, *d_syn_a = nullptr, *d_syn_b = nullptr;
   float *d_pattern = nullptr, *d_sharpen = nullptr;
   float2* d_gs = nullptr;
@@ -277,6 +277,8 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
     sa.seam_b = e->d_seam;
     sa.seam_t = e->d_seam ? e->d_seam + (size_t)(sa.segs - 1) * (a.g.bh / 2) * sa.seam_w : nullptr;
     sa.prefetch = e->sweep_prefetch;
+    sa.tab = e->d_tc;
+    sa.err = e->d_err;
     cudaEventRecord(e->ev[2], e->stream);
     cudaError_t ce = launch_sweep(e->inv_form, sa, e->stream);
     cudaEventRecord(e->ev[4], e->stream);
@@ -393,7 +395,11 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
   e->grid = make_grid(ip);
   e->device = device;
   e->form = form;
-  e->inv_form = form == F3D_FORM_TC ? F3D_FORM_FAST : form;
+  // The tensor-core sweep covers half-overlap mode 1 with 32x32 blocks; other
+  // tensor-core geometries pair its forward with the fast-form inverse.
+  e->inv_form = form;
+  if (form == F3D_FORM_TC && !(ip.ow * 2 == ip.bw && ip.oh * 2 == ip.bh)) e->inv_form = F3D_FORM_FAST;
+  if (form == F3D_FORM_TC && opts && (opts->flags & F3D_FLAG_UNFUSED)) e->inv_form = F3D_FORM_FAST;
   e->fbw = ip.bw / 2 + 1;
   e->ps = e->fbw * ip.bh;
   e->spec_bytes = sizeof(float2) * (size_t)e->grid.nb * e->ps;
@@ -424,7 +430,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
     e->gs = std::move(t.gs);
     if (ip.mode == 1) {
       std::vector<float> a, sa, sb;
-      windows_mode1(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, a, sa, sb, &e->win_ax, &e->win_ay);
+      windows_mode1(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, a, sa, sb, &e->axes);
     }
   }
 
@@ -460,7 +466,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
       (ce = up(reinterpret_cast<float**>(&e->d_gs), e->gs)) != cudaSuccess)
     return finish_fail(e->cuda_fail(ce, "table upload"));
   if (form == F3D_FORM_TC) {
-    const std::vector<uint8_t> tab = tc_tables(ip.bw, e->win_ax, e->win_ay, e->syn_a, e->syn_b);
+    const std::vector<uint8_t> tab = tc_tables(ip.bw, e->axes.ax, e->axes.ay, e->axes.sxa, e->axes.sxb, e->axes.sy);
     if (tab.empty()) return finish_fail(e->fail(F3D_E_UNSUPPORTED, "FFT3DCL: no tensor-core tables for this block size"));
     e->tc_bytes = tab.size();
     if ((ce = e->alloc(&e->d_tc, e->tc_bytes)) != cudaSuccess ||
@@ -483,7 +489,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
   if (!(opts && (opts->flags & F3D_FLAG_UNFUSED)) && sweep_supported(e->inv_form, geo, ip.bm)) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    sweep_plan(geo, sms > 0 ? sms : 1, &e->sweep_strips, &e->sweep_segs);
+    sweep_plan(e->inv_form, geo, sms > 0 ? sms : 1, &e->sweep_strips, &e->sweep_segs);
     e->seam_floats = sweep_seam_floats(geo, e->sweep_segs);
     if (e->seam_floats && (ce = e->alloc(&e->d_seam, sizeof(float) * e->seam_floats)) != cudaSuccess)
       return finish_fail(e->cuda_fail(ce, "seam buffer allocation"));

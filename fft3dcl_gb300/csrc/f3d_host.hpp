@@ -175,11 +175,14 @@ inline std::vector<float> window_mode0(int bw, int bh) {
 
 // buildWindowsMode1, src/cpu/tables.cpp:21-105, plus the odd-parity synthesis
 // window shifted by (bw-ow), src/cpu/reference.cpp:51-57.
-// The analysis window is separable: A[y][x] = float(ax[x] * ay[y]); ax and
-// ay (double) are returned when asked for.
+// The windows are separable: A[y][x] = float(ax[x] * ay[y]), synA[y][x] =
+// float(sxa[x] * sy[y]), synB[y][x] = float(sxb[x] * sy[y]) (sxb includes
+// the odd grid's shift).
+struct Mode1Axes {
+  std::vector<double> ax, ay, sxa, sxb, sy;
+};
 inline void windows_mode1(int bw, int bh, int ow, int oh, int wintype, std::vector<float>& A,
-                          std::vector<float>& synA, std::vector<float>& synB,
-                          std::vector<double>* ax = nullptr, std::vector<double>* ay = nullptr) {
+                          std::vector<float>& synA, std::vector<float>& synB, Mode1Axes* axes = nullptr) {
   std::vector<double> wanx(ow), wany(oh), wsynx(ow), wsyny(oh);
   auto half_cos = [](int i, int o) { return std::cos(kPi * (i - o + 0.5) / (o * 2.0)); };
   for (int i = 0; i < ow; i++) {
@@ -236,8 +239,12 @@ inline void windows_mode1(int bw, int bh, int ow, int oh, int wintype, std::vect
       wySA[ly] = wsyny[bh - 1 - ly];
     }
   }
-  if (ax) *ax = wxA;
-  if (ay) *ay = wyA;
+  if (axes) {
+    // synB below is sb shifted cyclically by bw - ow along x.
+    std::vector<double> sxb(bw);
+    for (int lx = 0; lx < bw; lx++) sxb[lx] = wxSB[(lx + bw - ow) % bw];
+    *axes = Mode1Axes{wxA, wyA, wxSA, sxb, wySA};
+  }
   A.assign(bw * bh, 0.0f);
   synA.assign(bw * bh, 0.0f);
   std::vector<float> sb(bw * bh);

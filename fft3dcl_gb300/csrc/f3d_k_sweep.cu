@@ -181,11 +181,8 @@ cudaError_t launch_bm(const SweepArgs& a, cudaStream_t st) {
   k<<<a.strips * a.segs, kSweepThreads, S_::SMEM, st>>>(a);
   count_launch();
   e = cudaGetLastError();
-  if (e != cudaSuccess || a.segs < 2) return e;
-  dim3 grid((a.inv.g.W + 255) / 256, BH / 2, a.segs - 1);
-  k_seam_merge<<<grid, 256, 0, st>>>(a, BH / 2);
-  count_launch();
-  return cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_seam_merge(a, st);
 }
 
 template <int BW, int BH>
@@ -202,20 +199,33 @@ cudaError_t launch_size(const SweepArgs& a, cudaStream_t st) {
 
 }  // namespace
 
+cudaError_t launch_seam_merge(const SweepArgs& a, cudaStream_t st) {
+  if (a.segs < 2) return cudaSuccess;
+  dim3 grid((a.inv.g.W + 255) / 256, a.inv.g.bh / 2, a.segs - 1);
+  k_seam_merge<<<grid, 256, 0, st>>>(a, a.inv.g.bh / 2);
+  count_launch();
+  return cudaGetLastError();
+}
+
 bool sweep_supported(int form, const Geo& g, int bm) {
-  if (form != F3D_FORM_FAST || bm == 0 || g.mode != 1) return false;
-  if (g.bw != g.bh || (g.bw != 8 && g.bw != 16 && g.bw != 32)) return false;
+  if (bm == 0 || g.mode != 1) return false;
+  if (form == F3D_FORM_TC) {
+    if (!tc_supported(g.mode, g.bw, g.bh, bm)) return false;
+  } else if (form != F3D_FORM_FAST || g.bw != g.bh || (g.bw != 8 && g.bw != 16 && g.bw != 32)) {
+    return false;
+  }
   return g.xoff == -g.bw / 2 && g.xstep == g.bw / 2 && g.yoff == -g.bh / 2 && g.ystep == g.bh / 2;
 }
 
-void sweep_plan(const Geo& g, int sm_count, int* strips, int* segs) {
-  const int tpb = g.bw, tj = kSweepThreads / tpb - 1;
+void sweep_plan(int form, const Geo& g, int sm_count, int* strips, int* segs) {
+  const int tj = form == F3D_FORM_TC ? kTcSweepCells : kSweepThreads / g.bw - 1;
+  const int per_sm = form == F3D_FORM_TC ? kTcSweepCtasPerSm : F3D_SWEEP_MINB;
   const int cells_x = (g.W + g.bw / 2 - 1) / (g.bw / 2);
   const int cells_y = (g.H + g.bh / 2 - 1) / (g.bh / 2);
   *strips = (cells_x + tj - 1) / tj;
   // At most one wave of resident CTAs (a partial second wave would double the
   // time), segments of at least two block rows.
-  int s = F3D_SWEEP_MINB * sm_count / *strips;
+  int s = per_sm * sm_count / *strips;
   const int maxseg = (cells_y + 1) / 2;
   if (s > maxseg) s = maxseg;
   *segs = s < 1 ? 1 : s;
@@ -228,6 +238,7 @@ size_t sweep_seam_floats(const Geo& g, int segs) {
 
 cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st) {
   if (!sweep_supported(form, a.inv.g, a.inv.bm)) return cudaErrorNotSupported;
+  if (form == F3D_FORM_TC) return launch_sweep_tc(a, st);
   switch (a.inv.g.bw) {
   case 8: return launch_size<8, 8>(a, st);
   case 16: return launch_size<16, 16>(a, st);

@@ -46,14 +46,16 @@ struct TcTab {
   static constexpr uint32_t B2HI = B1LO + N * N * 2, B2LO = B2HI + 8 * N * N;
   static constexpr uint32_t WSPEC = B2LO + 8 * N * N;  // float2 [N][FBW]
   static constexpr uint32_t C2HI = WSPEC + N * FBW * 8, C2LO = C2HI + 8 * N * N;
-  static constexpr uint32_t C1HI = C2LO + 8 * N * N, C1LO = C1HI + N * N * 2;
-  static constexpr uint32_t SYNA = C1LO + N * N * 2, SYNB = SYNA + N * N * 4;  // float [N][N]
-  static constexpr uint32_t TOTAL = SYNB + N * N * 4;
-  static_assert(WSPEC % 16 == 0 && C2HI % 16 == 0 && SYNA % 16 == 0, "16-byte sections");
+  // Row inverses with the even (A) and odd (B) synthesis x-windows.
+  static constexpr uint32_t C1AHI = C2LO + 8 * N * N, C1ALO = C1AHI + N * N * 2;
+  static constexpr uint32_t C1BHI = C1ALO + N * N * 2, C1BLO = C1BHI + N * N * 2;
+  static constexpr uint32_t TOTAL = C1BLO + N * N * 2;
+  static_assert(WSPEC % 16 == 0 && C2HI % 16 == 0 && C1AHI % 16 == 0, "16-byte sections");
 };
 
-// Scale of the filtered spectrum before its hi/lo split in the inverse,
-// undone in the synthesis window: keeps the column sums inside fp16 range.
+// Scale of the filtered spectrum before its hi/lo split in the inverse
+// (keeps the column sums inside fp16 range), undone with the inverse's
+// 1/n^2 when the blocks are added up.
 constexpr float kInvPre = 1.0f / 16.0f;
 
 // Kernel configuration for n x n blocks.
@@ -361,6 +363,330 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
   if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
+// ---- sweep: filter + inverse + overlap-add ------------------------------------
+//
+// The tensor-core counterpart of the fast-form sweep (f3d_k_sweep.cu): a CTA
+// owns a strip of TJ = 7 cells (block columns J0..J0+7, the last one the
+// strip's right neighbour) and a segment of block rows. Per block row, the 8
+// blocks of the strip form one group:
+//   F: the temporal filter (filter_bin_t, fast form) of the group's 8 x 544
+//      bins, contiguous in HBM, into shared memory;
+//   R: rows (k', block) of the column-inverse operand, k' = 0 packing the
+//      Hermitian parts of columns 0 and n/2 as H0 + i H(n/2), scaled by
+//      kInvPre and split hi/lo;
+//   step 2': V[y][k'] = sum_ky e^(2 pi i ky y/n) sy[y] F[ky][k'] (tensor cores);
+//   V: V into the row-inverse operand, rows (y, block slot) of two tiles
+//      that hold the even and the odd block columns;
+//   step 1': out[y][x] = sum_j V'[y][j] C1[x][j] with the even or odd
+//      synthesis x-window (tensor cores), i.e. fft2dRealInverseHalf
+//      (src/cpu/fft.cpp:88-119) times the synthesis window;
+//   O: overlap-add from tensor memory into the cell partial sums in the
+//      reference's block order (src/cpu/reference.cpp:415-436), finished cell
+//      rows packed straight to the output plane; segment seams as in the
+//      fast-form sweep.
+template <int N>
+struct SwpCfg {
+  using C = TcCfg<N>;
+  static constexpr int TJ = C::G - 1;        // cells per strip
+  static constexpr int CH = N / 2, CW = N / 2;
+  static constexpr int FS = C::PS + 4;       // filtered-bin stride per block (float2), padded
+  static constexpr int PR = CW + 4;          // partial-sum row stride (floats), padded
+  static constexpr int PC = CH * PR + 4;     // partial-sum cell stride (floats), padded
+  static constexpr uint32_t C2 = 0;                                  // hi, lo
+  static constexpr uint32_t C1 = C2 + 2 * C::B2_BYTES;               // A hi, A lo, B hi, B lo
+  static constexpr uint32_t A2 = (C1 + 4 * C::B1_BYTES + 1023) / 1024 * 1024;  // hi, lo (SWIZZLE_128B)
+  static constexpr uint32_t A1 = A2 + 2 * C::A2_BYTES;               // [tile][hi, lo] (INTERLEAVE)
+  static constexpr uint32_t FBUF = A1;                               // filtered bins (until R)
+  static constexpr uint32_t A1_END =
+      A1 + (2 * C::T1 * C::A1_BYTES > C::G * FS * 8 ? 2 * C::T1 * C::A1_BYTES : C::G * FS * 8);
+  static constexpr uint32_t P = A1_END;                              // [2][TJ][PC] floats
+  static constexpr uint32_t DC = P + 2 * TJ * PC * 4;                // [G] floats
+  static constexpr uint32_t BAR = DC + C::G * 4;
+  static constexpr uint32_t TSLOT = BAR + 16;
+  static constexpr uint32_t BYTES = TSLOT + 16 + 1024;
+  static_assert(C::T1 == 2, "one tile per block-column parity");
+  static_assert(BAR % 8 == 0 && P % 16 == 0, "alignment");
+};
+
+// Scale of a block sample after step 1': the inverse's 1/n^2 and kInvPre.
+template <int N>
+__host__ __device__ constexpr float out_scale() {
+  return 1.0f / (kInvPre * N * N);
+}
+
+// Packs and stores samples x0.. x0+15 of plane row y (bounds-checked).
+__device__ __forceinline__ void emit16(const SweepArgs& sa, int y, int x0, const float (&v)[16]) {
+  if (y >= sa.inv.g.H) return;
+  uint8_t* row = sa.dst + (long long)y * sa.pitch;
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    if (x0 + k >= sa.inv.g.W) break;
+    float s = v[k];
+    if (sa.chroma_norm != 0.0f) s += sa.chroma_norm;
+    store_sample(row, x0 + k, s, sa.fmt, sa.inv_norm, sa.max_pix);
+  }
+}
+
+template <int N, int BM>
+__global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constant__ SweepArgs sa) {
+  using C = TcCfg<N>;
+  using S = SwpCfg<N>;
+  using T = TcTab<N>;
+  const InvArgs& a = sa.inv;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  const uint32_t sbase = tc::smem_u32(sm);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::BAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::TSLOT);
+  float2* fbuf = reinterpret_cast<float2*>(sm + S::FBUF);
+  float* dcs = reinterpret_cast<float*>(sm + S::DC);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  const int strip = blockIdx.x % sa.strips, seg = blockIdx.x / sa.strips;
+  const int J0 = strip * S::TJ;
+  const int nrow = sa.cells_y + 1;
+  const int M0 = (int)((long long)seg * nrow / sa.segs);
+  const int M1 = (int)((long long)(seg + 1) * nrow / sa.segs);
+  const int ncell = min(S::TJ, sa.cells_x - J0);
+  const int ncols = a.g.ncols;
+
+  // Constant operands: C2 (hi, lo), then C1 A (hi, lo) and B (hi, lo).
+  {
+    const uint4* src2 = reinterpret_cast<const uint4*>(sa.tab + T::C2HI);
+    uint4* dst2 = reinterpret_cast<uint4*>(sm + S::C2);
+    for (int i = tid; i < (int)(2 * C::B2_BYTES / 16); i += kTcThreads) dst2[i] = src2[i];
+    const uint4* src1 = reinterpret_cast<const uint4*>(sa.tab + T::C1AHI);
+    uint4* dst1 = reinterpret_cast<uint4*>(sm + S::C1);
+    for (int i = tid; i < (int)(4 * C::B1_BYTES / 16); i += kTcThreads) dst1[i] = src1[i];
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, C::TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    tc::mbar_init(&bar[0], 1);
+    tc::mbar_init(&bar[1], 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  uint32_t phase = 0;
+  float* P_old = reinterpret_cast<float*>(sm + S::P);
+  float* P_new = P_old + S::TJ * S::PC;
+
+  for (int m = M0; m < M1; m++) {
+    // F. Temporal filter of the group's bins into shared memory.
+    if (tid < C::G) {
+      const int n = J0 + tid;
+      dcs[tid] = (n <= sa.cells_x && n < ncols) ? block_dc(a, m * ncols + n) : 0.0f;
+    }
+    __syncthreads();
+    {
+      const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
+#pragma unroll 4
+      for (int j = 0; j < C::G * C::PS / kTcThreads; j++) {
+        const int i = tid + kTcThreads * j;
+        const int bl = i / C::PS, li = i - bl * C::PS;
+        const int n = J0 + bl;
+        float2 f = make_float2(0.0f, 0.0f);
+        if (n <= sa.cells_x && n < ncols) f = filter_bin_t<BM, true>(a, dcs[bl], li, gb0 + i);
+        fbuf[bl * S::FS + li] = f;
+      }
+    }
+    __syncthreads();
+
+    // R. Column-inverse operand: row (k', block), K = 2 ky + (re, im).
+    {
+      const int r2 = tid & 127, h = tid >> 7;
+      const int kp = r2 >> 3, bl = r2 & 7;
+      const float2* fb = fbuf + bl * S::FS;
+#pragma unroll
+      for (int cq = 0; cq < C::NY / 4; cq++) {  // 4 ky (one 16-byte chunk) per step
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int ky = (C::NY) * h + 4 * cq + u;
+          float2 z;
+          if (kp == 0) {
+            const int kym = (N - ky) & (N - 1);
+            const float2 f0 = fb[ky * C::FBW], f0m = fb[kym * C::FBW];
+            const float2 fn = fb[ky * C::FBW + C::NY], fnm = fb[kym * C::FBW + C::NY];
+            const float h0x = 0.5f * (f0.x + f0m.x), h0y = 0.5f * (f0.y - f0m.y);
+            const float hnx = 0.5f * (fn.x + fnm.x), hny = 0.5f * (fn.y - fnm.y);
+            z = make_float2(h0x - hny, h0y + hnx);
+          } else {
+            z = fb[ky * C::FBW + kp];
+          }
+          tc::split_pair(z.x * kInvPre, z.y * kInvPre, hi[u], lo[u]);
+        }
+        const uint32_t o = tc::off_sw128(r2, 2 * (C::NY * h + 4 * cq));
+        *reinterpret_cast<uint4*>(sm + S::A2 + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(sm + S::A2 + C::A2_BYTES + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+
+    // Step 2' on the tensor cores: D2 = A2 * C2^T, three passes.
+    if (tid == 0) {
+      tc::fence_after_sync();
+      constexpr uint32_t id2 = tc::idesc_f16(128, C::N2);
+      const uint32_t sbo_b = (C::K2 / 8) * 128;
+      const uint32_t d = tmem + C::D2_COL;
+      for (int ks = 0; ks < C::K2 / 16; ks++) {
+        const uint64_t ah = tc::sdesc(sbase + S::A2 + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+        const uint64_t al = tc::sdesc(sbase + S::A2 + C::A2_BYTES + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+        const uint64_t bh = tc::sdesc(sbase + S::C2 + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
+        const uint64_t bl = tc::sdesc(sbase + S::C2 + C::B2_BYTES + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
+        tc::mma_f16(d, ah, bh, id2, ks > 0);
+        tc::mma_f16(d, ah, bl, id2, 1);
+        tc::mma_f16(d, al, bh, id2, 1);
+      }
+      tc::mma_commit(&bar[0]);
+    }
+    if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
+      if (tid == 0) atomicOr(sa.err, 1);
+      break;
+    }
+    tc::fence_after_sync();
+
+    // V. Row-inverse operand: tile = parity of the block column, row (y, slot).
+    {
+      const int s = warp & 3, h = warp >> 2;
+      const int r2 = 32 * s + lane;
+      const int kp = r2 >> 3, bl = r2 & 7;
+      const int tile = (J0 + bl) & 1, slot = bl >> 1;
+      uint8_t* t0 = sm + S::A1 + tile * 2 * C::A1_BYTES;
+      float v[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + 32 * h, v);
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const int y = 16 * h + j;
+        uint32_t hi, lo;
+        tc::split_pair(v[2 * j], v[2 * j + 1], hi, lo);
+        const uint32_t o = tc::off_il(4 * y + slot, 2 * kp, C::K1);
+        *reinterpret_cast<uint32_t*>(t0 + o) = hi;
+        *reinterpret_cast<uint32_t*>(t0 + C::A1_BYTES + o) = lo;
+      }
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+
+    // Step 1' on the tensor cores: D1[tile] = A1[tile] * C1(tile)^T.
+    if (tid == 0) {
+      tc::fence_after_sync();
+      constexpr uint32_t id1 = tc::idesc_f16(128, C::N1);
+      const uint32_t sbo = (C::K1 / 8) * 128;
+      for (int t = 0; t < C::T1; t++) {
+        const uint32_t a_hi = sbase + S::A1 + t * 2 * C::A1_BYTES, a_lo = a_hi + C::A1_BYTES;
+        const uint32_t b_hi = sbase + S::C1 + t * 2 * C::B1_BYTES, b_lo = b_hi + C::B1_BYTES;
+        const uint32_t d = tmem + C::D1_COL + t * C::N1;
+        for (int ks = 0; ks < C::K1 / 16; ks++) {
+          const uint64_t ah = tc::sdesc(a_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+          const uint64_t al = tc::sdesc(a_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+          const uint64_t bh = tc::sdesc(b_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+          const uint64_t bl = tc::sdesc(b_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+          tc::mma_f16(d, ah, bh, id1, ks > 0);
+          tc::mma_f16(d, ah, bl, id1, 1);
+          tc::mma_f16(d, al, bh, id1, 1);
+        }
+      }
+      tc::mma_commit(&bar[1]);
+    }
+    if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
+      if (tid == 0) atomicOr(sa.err, 1);
+      break;
+    }
+    phase ^= 1;
+    tc::fence_after_sync();
+
+    // O. Overlap-add. Thread: block row y of block bl; y < n/2 finishes cell
+    // row m-1 (P_old), y >= n/2 starts cell row m (P_new).
+    {
+      const int t = warp >> 2, s = warp & 3;
+      const int r = 32 * s + lane;
+      const int y = r >> 2, slot = r & 3;
+      const int bl = 2 * slot + ((t ^ J0) & 1);
+      float v[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
+#pragma unroll
+      for (int x = 0; x < 32; x++) v[x] *= out_scale<N>();
+      const bool top = y < S::CH;
+      const int yy = top ? y : y - S::CH;
+      const bool right_ok = bl < ncell;                // right half -> cell bl
+      const bool left_ok = bl >= 1 && bl - 1 < ncell;  // left half -> cell bl-1
+      const bool seam_top = m == M0;                   // cell row m-1 is another segment's (or none)
+      if (top) {
+        if (seam_top) {
+          if (M0 > 0 && right_ok) {
+            float* t0 = sa.seam_t + ((size_t)((seg - 1) * 2) * S::CH + yy) * sa.seam_w + (J0 + bl) * S::CW;
+#pragma unroll
+            for (int x = 0; x < S::CW; x += 4)
+              *reinterpret_cast<float4*>(t0 + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
+          }
+        } else if (right_ok) {
+          float* p = P_old + bl * S::PC + yy * S::PR;
+#pragma unroll
+          for (int x = 0; x < S::CW; x += 4) {
+            float4 q = *reinterpret_cast<float4*>(p + x);
+            q.x += v[16 + x], q.y += v[17 + x], q.z += v[18 + x], q.w += v[19 + x];
+            *reinterpret_cast<float4*>(p + x) = q;
+          }
+        }
+      } else if (right_ok) {
+        float* p = P_new + bl * S::PC + yy * S::PR;
+#pragma unroll
+        for (int x = 0; x < S::CW; x += 4)
+          *reinterpret_cast<float4*>(p + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
+      }
+      __syncthreads();
+      if (top) {
+        if (seam_top) {
+          if (M0 > 0 && left_ok) {
+            float* t1 = sa.seam_t + ((size_t)((seg - 1) * 2 + 1) * S::CH + yy) * sa.seam_w + (J0 + bl - 1) * S::CW;
+#pragma unroll
+            for (int x = 0; x < S::CW; x += 4)
+              *reinterpret_cast<float4*>(t1 + x) = make_float4(v[x], v[x + 1], v[x + 2], v[x + 3]);
+          }
+        } else if (left_ok) {
+          const float* p = P_old + (bl - 1) * S::PC + yy * S::PR;
+          float o[16];
+#pragma unroll
+          for (int x = 0; x < S::CW; x += 4) {
+            const float4 q = *reinterpret_cast<const float4*>(p + x);
+            o[x] = q.x + v[x], o[x + 1] = q.y + v[x + 1], o[x + 2] = q.z + v[x + 2], o[x + 3] = q.w + v[x + 3];
+          }
+          emit16(sa, (m - 1) * S::CH + yy, (J0 + bl - 1) * S::CW, o);
+        }
+      } else if (left_ok) {
+        float* p = P_new + (bl - 1) * S::PC + yy * S::PR;
+        const bool seam_bot = m == M1 - 1 && seg < sa.segs - 1;
+        float* sb = sa.seam_b + ((size_t)seg * S::CH + yy) * sa.seam_w + (J0 + bl - 1) * S::CW;
+#pragma unroll
+        for (int x = 0; x < S::CW; x += 4) {
+          float4 q = *reinterpret_cast<float4*>(p + x);
+          q.x += v[x], q.y += v[x + 1], q.z += v[x + 2], q.w += v[x + 3];
+          if (seam_bot) *reinterpret_cast<float4*>(sb + x) = q;
+          else *reinterpret_cast<float4*>(p + x) = q;
+        }
+      }
+    }
+    float* tmp = P_old;
+    P_old = P_new;
+    P_new = tmp;
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
+}
+
 template <class K>
 cudaError_t prepare(K k, size_t smem) {
   return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -387,7 +713,8 @@ void put_pair(std::vector<uint8_t>& t, uint32_t hi_base, uint32_t lo_base, uint3
 
 template <int N>
 std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<double>& wy,
-                              const std::vector<float>& syn_a, const std::vector<float>& syn_b) {
+                              const std::vector<double>& sxa, const std::vector<double>& sxb,
+                              const std::vector<double>& sy) {
   using T = TcTab<N>;
   constexpr int NY = N / 2, FBW = NY + 1;
   std::vector<uint8_t> t(T::TOTAL, 0);
@@ -396,20 +723,18 @@ std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<d
     c = std::cos(th);
     s = std::sin(th);
   };
-  // B1 [j][x]: packed real row DFT with wx folded in.
+  // Packed real row transform coefficient j at x: 1, (-1)^x, cos, -sin.
+  auto row_coef = [&](int j, int x) {
+    if (j == 0) return 1.0;
+    if (j == 1) return (x & 1) ? -1.0 : 1.0;
+    double c, s;
+    cs(j / 2, x, c, s);
+    return (j & 1) ? -s : c;
+  };
+  // B1 [j][x]: packed real row DFT, analysis x-window folded in.
   for (int j = 0; j < N; j++)
-    for (int x = 0; x < N; x++) {
-      double v;
-      if (j == 0) v = 1.0;
-      else if (j == 1) v = (x & 1) ? -1.0 : 1.0;
-      else {
-        double c, s;
-        cs(j / 2, x, c, s);
-        v = (j & 1) ? -s : c;
-      }
-      put_pair(t, T::B1HI, T::B1LO, tc::off_il(j, x, N), v * wx[x]);
-    }
-  // B2 [2ky+ro][2y+ri]: complex column DFT with wy folded in.
+    for (int x = 0; x < N; x++) put_pair(t, T::B1HI, T::B1LO, tc::off_il(j, x, N), row_coef(j, x) * wx[x]);
+  // B2 [2ky+ro][2y+ri]: complex column DFT, analysis y-window folded in.
   for (int ky = 0; ky < N; ky++)
     for (int y = 0; y < N; y++) {
       double c, s;
@@ -433,36 +758,26 @@ std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<d
       const float f[2] = {(float)re, (float)im};
       std::memcpy(t.data() + T::WSPEC + (ky * FBW + kx) * 8, f, 8);
     }
-  // C2 [2y+ro][2ky+ri]: complex column inverse DFT (unnormalised).
+  // C2 [2y+ro][2ky+ri]: complex column inverse DFT (unnormalised), synthesis
+  // y-window folded in.
   for (int y = 0; y < N; y++)
     for (int ky = 0; ky < N; ky++) {
       double c, s;
       cs(ky, y, c, s);
-      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y, 2 * ky, 2 * N), c);
-      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y, 2 * ky + 1, 2 * N), -s);
-      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y + 1, 2 * ky, 2 * N), s);
-      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y + 1, 2 * ky + 1, 2 * N), c);
+      const double w = sy[y];
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y, 2 * ky, 2 * N), w * c);
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y, 2 * ky + 1, 2 * N), -w * s);
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y + 1, 2 * ky, 2 * N), w * s);
+      put_pair(t, T::C2HI, T::C2LO, tc::off_il(2 * y + 1, 2 * ky + 1, 2 * N), w * c);
     }
-  // C1 [x][j]: real row inverse from the packed half spectrum.
+  // C1 [x][j]: real row inverse from the packed half spectrum (twice the
+  // cos/sin terms: the mirrored columns), synthesis x-window folded in.
   for (int x = 0; x < N; x++)
     for (int j = 0; j < N; j++) {
-      double v;
-      if (j == 0) v = 1.0;
-      else if (j == 1) v = (x & 1) ? -1.0 : 1.0;
-      else {
-        double c, s;
-        cs(j / 2, x, c, s);
-        v = (j & 1) ? -2.0 * s : 2.0 * c;
-      }
-      put_pair(t, T::C1HI, T::C1LO, tc::off_il(x, j, N), v);
+      const double v = j < 2 ? row_coef(j, x) : 2.0 * row_coef(j, x);
+      put_pair(t, T::C1AHI, T::C1ALO, tc::off_il(x, j, N), v * sxa[x]);
+      put_pair(t, T::C1BHI, T::C1BLO, tc::off_il(x, j, N), v * sxb[x]);
     }
-  // Synthesis windows with the inverse's 1/n^2 and the pre-scale undone.
-  const float k = 1.0f / (kInvPre * N * N);
-  for (int i = 0; i < N * N; i++) {
-    const float fa = syn_a.empty() ? 0.0f : syn_a[i] * k, fb = syn_b.empty() ? 0.0f : syn_b[i] * k;
-    std::memcpy(t.data() + T::SYNA + i * 4, &fa, 4);
-    std::memcpy(t.data() + T::SYNB + i * 4, &fb, 4);
-  }
   return t;
 }
 
@@ -471,8 +786,11 @@ std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<d
 bool tc_supported(int mode, int bw, int bh, int bm) { return mode == 1 && bw == 32 && bh == 32 && bm != 0; }
 
 std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::vector<double>& wy,
-                               const std::vector<float>& syn_a, const std::vector<float>& syn_b) {
-  if (n == 32 && (int)wx.size() == n && (int)wy.size() == n) return tables_n<32>(wx, wy, syn_a, syn_b);
+                               const std::vector<double>& sxa, const std::vector<double>& sxb,
+                               const std::vector<double>& sy) {
+  for (const auto* v : {&wx, &wy, &sxa, &sxb, &sy})
+    if ((int)v->size() != n) return {};
+  if (n == 32) return tables_n<32>(wx, wy, sxa, sxb, sy);
   return {};
 }
 
@@ -489,6 +807,33 @@ cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st) {
   k<<<grid, kTcThreads, smem, st>>>(a);
   count_launch();
   return cudaGetLastError();
+}
+
+template <int BM>
+cudaError_t launch_sweep_bm(const SweepArgs& a, cudaStream_t st) {
+  constexpr size_t smem = SwpCfg<32>::BYTES;
+  static_assert(kTcSweepCtasPerSm * (SwpCfg<32>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
+  static_assert(SwpCfg<32>::TJ == kTcSweepCells, "cells per strip");
+  auto k = k_sweep_tc<32, BM>;
+  cudaError_t e = prepare(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<a.strips * a.segs, kTcThreads, smem, st>>>(a);
+  count_launch();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_seam_merge(a, st);
+}
+
+cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st) {
+  if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err) return cudaErrorNotSupported;
+  switch (a.inv.bm) {
+  case -1: return launch_sweep_bm<-1>(a, st);
+  case 1: return launch_sweep_bm<1>(a, st);
+  case 2: return launch_sweep_bm<2>(a, st);
+  case 3: return launch_sweep_bm<3>(a, st);
+  case 4: return launch_sweep_bm<4>(a, st);
+  default: return cudaErrorNotSupported;
+  }
 }
 
 }  // namespace f3d

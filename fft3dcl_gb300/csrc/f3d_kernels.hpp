@@ -91,12 +91,14 @@ struct SweepArgs {
   int prefetch;          // L2 prefetch of the next block row: 0 off, 1 at row start, 2 after the filter
   float* seam_b;         // [segs-1][bh/2][seam_w]: first two quadrants of each seam cell, summed
   float* seam_t;         // [segs-1][2][bh/2][seam_w]: third and fourth quadrants
+  const uint8_t* tab;    // tensor-core form: device copy of tc_tables()
+  int* err;              // tensor-core form: set non-zero when a wait gives up
 };
 
 // Whether the sweep handles this geometry and form; its CTA grid; the seam
 // scratch it needs (floats); and the launches (sweep, then merge).
 bool sweep_supported(int form, const Geo& g, int bm);
-void sweep_plan(const Geo& g, int sm_count, int* strips, int* segs);
+void sweep_plan(int form, const Geo& g, int sm_count, int* strips, int* segs);
 size_t sweep_seam_floats(const Geo& g, int segs);
 cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st);
 
@@ -139,12 +141,20 @@ struct TcFwdArgs {
   int* err;            // set non-zero when a tensor-core wait gives up
 };
 bool tc_supported(int mode, int bw, int bh, int bm);
-// DFT matrices (fp16 hi/lo, in the kernels' shared-memory operand layout),
-// the analysis window's spectrum and the scaled synthesis windows, for
-// n x n blocks whose mode-1 analysis window is wx[x] * wy[y].
+// DFT matrices (fp16 hi/lo, in the kernels' shared-memory operand layout)
+// with the separable mode-1 windows folded in, and the analysis window's
+// spectrum, for n x n blocks: analysis wx[x] * wy[y], synthesis sxa[x] *
+// sy[y] (even block columns) and sxb[x] * sy[y] (odd).
 std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::vector<double>& wy,
-                               const std::vector<float>& syn_a, const std::vector<float>& syn_b);
+                               const std::vector<double>& sxa, const std::vector<double>& sxb,
+                               const std::vector<double>& sy);
 cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st);
+// Tensor-core sweep: cells per strip, CTAs per SM, and the launch (with the
+// seam merge of f3d_k_sweep.cu).
+constexpr int kTcSweepCells = 7;
+constexpr int kTcSweepCtasPerSm = 2;
+cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st);
+cudaError_t launch_seam_merge(const SweepArgs& a, cudaStream_t st);
 
 // Counts one kernel launch made by this library (all engines, all threads).
 void count_launch();

@@ -116,3 +116,23 @@ def test_form_golden_within_tolerance(form, path):
     frames, out, bits, chroma, params = load_case(path)
     got = gpu_clip(frames, bits, chroma=chroma, form=form, **params)
     check(got, out, tol_for(frames, bits))
+
+
+@pytest.mark.parametrize("w,h,params", [
+    (640, 360, dict(bt=3)),
+    (333, 177, dict(bt=2, sharpen=0.5)),
+    (1000, 37, dict(bt=-1, sharpen=0.3)),
+    (41, 700, dict(bt=4, sigma2=1.0, sigma3=3.0, sigma4=4.0)),
+    (1920, 1080, dict(bt=1, degrid=0.0)),
+])
+def test_tc_sweep_sizes(w, h, params):
+    # The tensor-core sweep on planes with ragged edges, one and many
+    # segments (seam rows) and strips, against the oracle.
+    frames = synth.moving_rects(w, h, 5, w + 3 * h, lo=16, hi=235, noise=4.0, n_rects=5)
+    flt = F.Filter([[f] for f in frames], F.VideoFormat("gray", 8, 0), form="tc", **params)
+    info = flt.engines[0].info()
+    assert info.form == 2 and info.fused == 1
+    got = [flt.get_frame(n)[0] for n in range(len(frames))]
+    flt.close()
+    ref = oracle.run_clip(frames, 8, threads=16, **params)
+    check(got, ref, 1)
