@@ -67,16 +67,22 @@ __device__ __forceinline__ float load_sample(const uint8_t* row, int x, int fmt,
 // Float to destination sample, src/cpu/reference.cpp:107-138. The product
 // and the +0.5 are rounded separately (no fused multiply-add), and the cast
 // truncates a non-negative value, i.e. floors it.
+__device__ __forceinline__ uint32_t pack_u8(float v) {
+  v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+  return __float2uint_rz(__fadd_rn(__fmul_rn(v, 255.0f), 0.5f));
+}
+__device__ __forceinline__ uint32_t pack_u16(float v, float inv_norm, float max_pix) {
+  v = __fmul_rn(v, inv_norm);
+  v = v < max_pix ? v : max_pix;
+  v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+  return __float2uint_rz(__fadd_rn(__fmul_rn(v, 65535.0f), 0.5f));
+}
 __device__ __forceinline__ void store_sample(uint8_t* row, int x, float v, int fmt, float inv_norm,
                                              float max_pix) {
   if (fmt == FMT_U8) {
-    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
-    row[x] = (uint8_t)__float2uint_rz(__fadd_rn(__fmul_rn(v, 255.0f), 0.5f));
+    row[x] = (uint8_t)pack_u8(v);
   } else if (fmt == FMT_U16) {
-    v = __fmul_rn(v, inv_norm);
-    v = v < max_pix ? v : max_pix;
-    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
-    reinterpret_cast<uint16_t*>(row)[x] = (uint16_t)__float2uint_rz(__fadd_rn(__fmul_rn(v, 65535.0f), 0.5f));
+    reinterpret_cast<uint16_t*>(row)[x] = (uint16_t)pack_u16(v, inv_norm, max_pix);
   } else {
     reinterpret_cast<float*>(row)[x] = v;
   }
@@ -92,6 +98,22 @@ __device__ __forceinline__ void wienner(float& re, float& im, float sx, float sy
   im *= mul;
 }
 
+// The same shrink for the fast forms. With sx = beta * sy (both the plain
+// and the pattern sigmas are built that way) the factor 1 - sy/psd passes
+// beta_x = 1 - 1/beta exactly at psd = sx and grows with psd, so the
+// reference's branch is max(1 - sy/psd, beta_x); psd = 0 gives -inf -> beta_x.
+template <bool FAST>
+__device__ __forceinline__ void wienner_t(float& re, float& im, float sx, float sy, float beta_x) {
+  if (!FAST) {
+    wienner(re, im, sx, sy, beta_x);
+    return;
+  }
+  const float psd = fmaf(re, re, im * im);
+  const float mul = fmaxf(fmaf(-sy, 1.0f / psd, 1.0f), beta_x);
+  re *= mul;
+  im *= mul;
+}
+
 // Temporal mode as a template argument: -1..4 fixed at compile time (no
 // branch, and no Kalman state stores in the other modes' code, so the
 // compiler may move spectra loads freely), kRuntimeBm to read a.bm.
@@ -103,14 +125,15 @@ __device__ __forceinline__ float block_dc(const InvArgs& a, int b) {
 }
 
 // Temporal filter + sharpen of bin i (0 <= i < bh*fbw) of a block whose
-// current-frame DC is dc, with gi = b*bh*fbw + i. Follows
+// current-frame DC is dc, with gi = b*bh*fbw + i and sv the bin's window
+// spectra (load_window). Follows
 // src/cpu/reference.cpp:229-409 per bin: degrid correction, bm 2/3/4
 // temporal DFT + Wiener, bm 1 Wiener, bm 0 Kalman (state updated in place),
 // bm -1 pass-through, then sharpen. FAST evaluates the 3- and 4-point
 // temporal transforms with fewer additions (a different rounding; the exact
 // form keeps the reference's expressions).
 template <int BM, bool FAST = false>
-__device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i, size_t gi) {
+__device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i, size_t gi, const float2 (&sv)[4]) {
   float d_re = 0.0f, d_im = 0.0f;
   if (a.dg) {
     const float2 g = a.gs[i];
@@ -126,15 +149,15 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
   float fr, fi;
   const int bm = BM == kRuntimeBm ? a.bm : BM;
   if (bm == 2) {
-    const float2 p = a.s[0][gi], c = a.s[1][gi];
+    const float2 p = sv[0], c = sv[1];
     float ar = c.x - p.x, ai = c.y - p.y;
     float br = c.x + p.x, bi = c.y + p.y;
     if (a.dg) {
       br -= 2.0f * d_re;
       bi -= 2.0f * d_im;
     }
-    wienner(ar, ai, sx, sy, a.beta_x);
-    wienner(br, bi, sx, sy, a.beta_x);
+    wienner_t<FAST>(ar, ai, sx, sy, a.beta_x);
+    wienner_t<FAST>(br, bi, sx, sy, a.beta_x);
     fr = (ar + br) * 0.5f;
     fi = (ai + bi) * 0.5f;
     if (a.dg) {
@@ -142,7 +165,7 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
       fi += d_im;
     }
   } else if (bm == 3) {
-    const float2 p = a.s[0][gi], c = a.s[1][gi], n = a.s[2][gi];
+    const float2 p = sv[0], c = sv[1], n = sv[2];
     const float K = 0.8660254f;  // truncated literal, src/cpu/reference.cpp:247
     float t1r = p.x + n.x, t1i = p.y + n.y;
     float y1r = c.x - 0.5f * t1r, y1i = c.y - 0.5f * t1i;
@@ -155,9 +178,9 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
       d1r -= 3.0f * d_re;
       d1i -= 3.0f * d_im;
     }
-    wienner(d0r, d0i, sx, sy, a.beta_x);
-    wienner(d1r, d1i, sx, sy, a.beta_x);
-    wienner(d2r, d2i, sx, sy, a.beta_x);
+    wienner_t<FAST>(d0r, d0i, sx, sy, a.beta_x);
+    wienner_t<FAST>(d1r, d1i, sx, sy, a.beta_x);
+    wienner_t<FAST>(d2r, d2i, sx, sy, a.beta_x);
     fr = (d0r + d1r + d2r) * (1.0f / 3.0f);
     fi = (d0i + d1i + d2i) * (1.0f / 3.0f);
     if (a.dg) {
@@ -165,7 +188,7 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
       fi += d_im;
     }
   } else if (bm == 4) {
-    const float2 p2 = a.s[0][gi], p1 = a.s[1][gi], c = a.s[2][gi], n = a.s[3][gi];
+    const float2 p2 = sv[0], p1 = sv[1], c = sv[2], n = sv[3];
     float fp1r, fp1i, fcr, fci, fnr, fni, fp2r, fp2i;
     if (FAST) {  // radix 2 x 2: (c +- p2), (p1 +- n)
       const float sr = c.x + p2.x, si = c.y + p2.y, dr = c.x - p2.x, di = c.y - p2.y;
@@ -186,10 +209,10 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
       fp1r -= 4.0f * d_re;
       fp1i -= 4.0f * d_im;
     }
-    wienner(fp2r, fp2i, sx, sy, a.beta_x);
-    wienner(fp1r, fp1i, sx, sy, a.beta_x);
-    wienner(fcr, fci, sx, sy, a.beta_x);
-    wienner(fnr, fni, sx, sy, a.beta_x);
+    wienner_t<FAST>(fp2r, fp2i, sx, sy, a.beta_x);
+    wienner_t<FAST>(fp1r, fp1i, sx, sy, a.beta_x);
+    wienner_t<FAST>(fcr, fci, sx, sy, a.beta_x);
+    wienner_t<FAST>(fnr, fni, sx, sy, a.beta_x);
     fr = (fp2r + fp1r + fcr + fnr) * 0.25f;
     fi = (fp2i + fp1i + fci + fni) * 0.25f;
     if (a.dg) {
@@ -197,13 +220,13 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
       fi += d_im;
     }
   } else if (bm == 1) {
-    const float2 c = a.s[0][gi];
+    const float2 c = sv[0];
     float re = c.x, im = c.y;
     if (a.dg) {
       re -= d_re;
       im -= d_im;
     }
-    wienner(re, im, sx, sy, a.beta_x);
+    wienner_t<FAST>(re, im, sx, sy, a.beta_x);
     if (a.dg) {
       re += d_re;
       im += d_im;
@@ -211,7 +234,7 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
     fr = re;
     fi = im;
   } else if (bm == 0) {
-    const float2 c = a.s[0][gi];
+    const float2 c = sv[0];
     const float cn = a.pat ? a.pattern[i] : a.kalman_cn;
     float2 l;
     float s;
@@ -242,7 +265,7 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
     fr = dst_r;
     fi = dst_i;
   } else {
-    const float2 c = a.s[0][gi];
+    const float2 c = sv[0];
     fr = c.x;
     fi = c.y;
   }
@@ -265,6 +288,23 @@ __device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i
     fi = im;
   }
   return make_float2(fr, fi);
+}
+
+// The window's spectra of bin gi, in temporal order (frames the mode reads).
+template <int BM>
+__device__ __forceinline__ void load_window(const InvArgs& a, size_t gi, float2 (&sv)[4]) {
+  const int bm = BM == kRuntimeBm ? a.bm : BM;
+  const int nf = bm >= 2 ? bm : 1;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (k < nf) sv[k] = a.s[k][gi];
+}
+
+template <int BM, bool FAST = false>
+__device__ __forceinline__ float2 filter_bin_t(const InvArgs& a, float dc, int i, size_t gi) {
+  float2 sv[4];
+  load_window<BM>(a, gi, sv);
+  return filter_vals<BM, FAST>(a, dc, i, gi, sv);
 }
 
 __device__ __forceinline__ float2 filter_bin(const InvArgs& a, int b, int i, size_t gi) {

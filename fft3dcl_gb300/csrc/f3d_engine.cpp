@@ -88,6 +88,8 @@ struct f3d_engine {
   int sweep_strips = 0, sweep_segs = 0, sweep_prefetch = 0;
   float* d_seam = nullptr;
   size_t seam_floats = 0;
+  uint8_t* d_img = nullptr;  // tensor-core sweep: filtered operand tiles
+  size_t img_bytes = 0;
 
   size_t bytes = 0;
   // Kernel timing on the engine stream: forward [0,1], filter+inverse [2,4],
@@ -279,6 +281,7 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
     sa.prefetch = e->sweep_prefetch;
     sa.tab = e->d_tc;
     sa.err = e->d_err;
+    sa.img = e->d_img;
     cudaEventRecord(e->ev[2], e->stream);
     cudaError_t ce = launch_sweep(e->inv_form, sa, e->stream);
     cudaEventRecord(e->ev[4], e->stream);
@@ -493,6 +496,11 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
     e->seam_floats = sweep_seam_floats(geo, e->sweep_segs);
     if (e->seam_floats && (ce = e->alloc(&e->d_seam, sizeof(float) * e->seam_floats)) != cudaSuccess)
       return finish_fail(e->cuda_fail(ce, "seam buffer allocation"));
+    if (e->inv_form == F3D_FORM_TC) {
+      e->img_bytes = tc_image_bytes(geo, e->sweep_strips);
+      if ((ce = e->alloc(&e->d_img, e->img_bytes)) != cudaSuccess)
+        return finish_fail(e->cuda_fail(ce, "tensor-core operand buffer allocation"));
+    }
     e->fused = true;
     const int fl = opts ? opts->flags : 0;
     e->sweep_prefetch = (fl & F3D_FLAG_PREFETCH_EARLY) ? 1 : (fl & F3D_FLAG_PREFETCH_LATE) ? 2 : 0;
@@ -512,6 +520,7 @@ void f3d_engine_destroy(f3d_engine* e) {
     e->pool.clear();
     e->release(e->d_win_ana, e->win_ana.size() * sizeof(float));
     e->release(e->d_tc, e->tc_bytes);
+    e->release(e->d_img, e->img_bytes);
     e->release(e->d_err, sizeof(int));
     e->release(e->d_syn_a, e->syn_a.size() * sizeof(float));
     e->release(e->d_syn_b, e->syn_b.size() * sizeof(float));

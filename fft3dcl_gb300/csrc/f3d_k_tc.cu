@@ -76,6 +76,10 @@ struct TcCfg {
 };
 
 constexpr int kTcThreads = 256;
+#ifndef F3D_TC_FILTER_BATCH
+#define F3D_TC_FILTER_BATCH 3
+#endif
+constexpr int kTcFilterBatch = F3D_TC_FILTER_BATCH;  // bins whose loads are in flight together
 constexpr uint64_t kWaitNs = 1000000000ull;  // one second
 
 // ---- forward ---------------------------------------------------------------
@@ -363,17 +367,24 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
   if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
-// ---- sweep: filter + inverse + overlap-add ------------------------------------
+// ---- sweep: filter, then inverse + overlap-add -------------------------------
 //
-// The tensor-core counterpart of the fast-form sweep (f3d_k_sweep.cu): a CTA
-// owns a strip of TJ = 7 cells (block columns J0..J0+7, the last one the
-// strip's right neighbour) and a segment of block rows. Per block row, the 8
-// blocks of the strip form one group:
-//   F: the temporal filter (filter_bin_t, fast form) of the group's 8 x 544
+// The tensor-core counterpart of the fast-form sweep (f3d_k_sweep.cu). The
+// plane is cut into strips of TJ = 7 cells; the group of a strip in block row
+// m is block columns J0..J0+7 (the last one the strip's right neighbour).
+//
+// k_filter_tc, one CTA per (row, strip) group:
+//   F: the temporal filter (filter_vals, fast form) of the group's 8 x 544
 //      bins, contiguous in HBM, into shared memory;
 //   R: rows (k', block) of the column-inverse operand, k' = 0 packing the
 //      Hermitian parts of columns 0 and n/2 as H0 + i H(n/2), scaled by
-//      kInvPre and split hi/lo;
+//      kInvPre and split hi/lo, written to HBM as the exact shared-memory
+//      image (SWIZZLE_128B) the inverse kernel loads with one bulk copy.
+// With no tensor-memory phases to wait for, it runs at three CTAs per SM.
+//
+// k_sweep_tc, one CTA per (strip, segment of block rows), per row:
+//   the operand tile arrives by bulk copy (issued while the previous row's
+//   transforms ran);
 //   step 2': V[y][k'] = sum_ky e^(2 pi i ky y/n) sy[y] F[ky][k'] (tensor cores);
 //   V: V into the row-inverse operand, rows (y, block slot) of two tiles
 //      that hold the even and the odd block columns;
@@ -392,18 +403,19 @@ struct SwpCfg {
   static constexpr int FS = C::PS + 4;       // filtered-bin stride per block (float2), padded
   static constexpr int PR = CW + 4;          // partial-sum row stride (floats), padded
   static constexpr int PC = CH * PR + 4;     // partial-sum cell stride (floats), padded
+  static constexpr uint32_t TILE = 2 * C::A2_BYTES;                  // operand image: hi, lo
+  // Inverse kernel shared memory.
   static constexpr uint32_t C2 = 0;                                  // hi, lo
   static constexpr uint32_t C1 = C2 + 2 * C::B2_BYTES;               // A hi, A lo, B hi, B lo
   static constexpr uint32_t A2 = (C1 + 4 * C::B1_BYTES + 1023) / 1024 * 1024;  // hi, lo (SWIZZLE_128B)
-  static constexpr uint32_t A1 = A2 + 2 * C::A2_BYTES;               // [tile][hi, lo] (INTERLEAVE)
-  static constexpr uint32_t FBUF = A1;                               // filtered bins (until R)
-  static constexpr uint32_t A1_END =
-      A1 + (2 * C::T1 * C::A1_BYTES > C::G * FS * 8 ? 2 * C::T1 * C::A1_BYTES : C::G * FS * 8);
-  static constexpr uint32_t P = A1_END;                              // [2][TJ][PC] floats
-  static constexpr uint32_t DC = P + 2 * TJ * PC * 4;                // [G] floats
-  static constexpr uint32_t BAR = DC + C::G * 4;
-  static constexpr uint32_t TSLOT = BAR + 16;
-  static constexpr uint32_t BYTES = TSLOT + 16 + 1024;
+  static constexpr uint32_t A1 = A2 + TILE;                          // [tile][hi, lo] (INTERLEAVE)
+  static constexpr uint32_t P = A1 + 2 * C::T1 * C::A1_BYTES;        // [2][TJ][PC] floats
+  static constexpr uint32_t BAR = P + 2 * TJ * PC * 4;               // operand load, step 2', step 1'
+  static constexpr uint32_t TSLOT = BAR + 24;
+  static constexpr uint32_t BYTES = TSLOT + 8 + 1024;
+  // Filter kernel shared memory.
+  static constexpr uint32_t F_DC = C::G * FS * 8;
+  static constexpr uint32_t F_BYTES = F_DC + C::G * 4;
   static_assert(C::T1 == 2, "one tile per block-column parity");
   static_assert(BAR % 8 == 0 && P % 16 == 0, "alignment");
 };
@@ -414,10 +426,32 @@ __host__ __device__ constexpr float out_scale() {
   return 1.0f / (kInvPre * N * N);
 }
 
-// Packs and stores samples x0.. x0+15 of plane row y (bounds-checked).
+// Packs and stores samples x0.. x0+15 of plane row y (bounds-checked), with
+// 16-byte stores where the run is inside the plane and aligned.
 __device__ __forceinline__ void emit16(const SweepArgs& sa, int y, int x0, const float (&v)[16]) {
   if (y >= sa.inv.g.H) return;
   uint8_t* row = sa.dst + (long long)y * sa.pitch;
+  const bool full = x0 + 16 <= sa.inv.g.W;
+  if (full && sa.fmt == FMT_U16 && ((reinterpret_cast<uintptr_t>(row) + 2 * x0) & 15) == 0) {
+    uint32_t w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      w[k] = pack_u16(v[2 * k] + sa.chroma_norm, sa.inv_norm, sa.max_pix) |
+             (pack_u16(v[2 * k + 1] + sa.chroma_norm, sa.inv_norm, sa.max_pix) << 16);
+    uint4* p = reinterpret_cast<uint4*>(row + 2 * x0);
+    p[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    p[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    return;
+  }
+  if (full && sa.fmt == FMT_U8 && ((reinterpret_cast<uintptr_t>(row) + x0) & 15) == 0) {
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      w[k] = pack_u8(v[4 * k] + sa.chroma_norm) | (pack_u8(v[4 * k + 1] + sa.chroma_norm) << 8) |
+             (pack_u8(v[4 * k + 2] + sa.chroma_norm) << 16) | (pack_u8(v[4 * k + 3] + sa.chroma_norm) << 24);
+    *reinterpret_cast<uint4*>(row + x0) = make_uint4(w[0], w[1], w[2], w[3]);
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < 16; k++) {
     if (x0 + k >= sa.inv.g.W) break;
@@ -428,18 +462,91 @@ __device__ __forceinline__ void emit16(const SweepArgs& sa, int y, int x0, const
 }
 
 template <int N, int BM>
+__global__ void __launch_bounds__(kTcThreads, 3) k_filter_tc(const __grid_constant__ SweepArgs sa) {
+  using C = TcCfg<N>;
+  using S = SwpCfg<N>;
+  const InvArgs& a = sa.inv;
+  extern __shared__ __align__(16) uint8_t smem_f[];
+  float2* fbuf = reinterpret_cast<float2*>(smem_f);
+  float* dcs = reinterpret_cast<float*>(smem_f + S::F_DC);
+  const int tid = threadIdx.x;
+  const int strip = blockIdx.x % sa.strips, m = blockIdx.x / sa.strips;
+  const int J0 = strip * S::TJ;
+  const int ncols = a.g.ncols;
+  const int nvbin = max(0, min(C::G, min(sa.cells_x + 1, ncols) - J0)) * C::PS;  // bins of needed blocks
+  constexpr int NBIN = C::G * C::PS;
+  constexpr int NB = NBIN / kTcThreads;
+  static_assert(NBIN % kTcThreads == 0, "bins per thread");
+
+  if (tid < C::G) {
+    const int n = J0 + tid;
+    dcs[tid] = (n <= sa.cells_x && n < ncols) ? block_dc(a, m * ncols + n) : 0.0f;
+  }
+  __syncthreads();
+
+  // F. Bins tid + 256 j; the loads of kTcFilterBatch bins are issued together.
+  const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
+#pragma unroll
+  for (int j0 = 0; j0 < NB; j0 += kTcFilterBatch) {
+    float2 sv[kTcFilterBatch][4];
+#pragma unroll
+    for (int u = 0; u < kTcFilterBatch; u++) {
+      const int i = tid + kTcThreads * (j0 + u);
+      if (j0 + u < NB && i < nvbin) load_window<BM>(a, gb0 + i, sv[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kTcFilterBatch; u++) {
+      if (j0 + u >= NB) continue;
+      const int i = tid + kTcThreads * (j0 + u);
+      const int bl = i / C::PS, li = i - bl * C::PS;
+      float2 f = make_float2(0.0f, 0.0f);
+      if (i < nvbin) f = filter_vals<BM, true>(a, dcs[bl], li, gb0 + i, sv[u]);
+      fbuf[bl * S::FS + li] = f;
+    }
+  }
+  __syncthreads();
+
+  // R. Row (k', block), K = 2 ky + (re, im) of the operand image, in 16-byte
+  // chunks of 4 ky.
+  uint8_t* img = sa.img + ((size_t)m * sa.strips + strip) * S::TILE;
+  const int r2 = tid & 127, h = tid >> 7;
+  const int kp = r2 >> 3, bl = r2 & 7;
+  const float2* fb = fbuf + bl * S::FS;
+#pragma unroll
+  for (int cq = 0; cq < C::NY / 4; cq++) {
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int ky = C::NY * h + 4 * cq + u;
+      float2 z;
+      if (kp == 0) {
+        const int kym = (N - ky) & (N - 1);
+        const float2 f0 = fb[ky * C::FBW], f0m = fb[kym * C::FBW];
+        const float2 fn = fb[ky * C::FBW + C::NY], fnm = fb[kym * C::FBW + C::NY];
+        const float h0x = 0.5f * (f0.x + f0m.x), h0y = 0.5f * (f0.y - f0m.y);
+        const float hnx = 0.5f * (fn.x + fnm.x), hny = 0.5f * (fn.y - fnm.y);
+        z = make_float2(h0x - hny, h0y + hnx);
+      } else {
+        z = fb[ky * C::FBW + kp];
+      }
+      tc::split_pair(z.x * kInvPre, z.y * kInvPre, hi[u], lo[u]);
+    }
+    const uint32_t o = tc::off_sw128(r2, 2 * (C::NY * h + 4 * cq));
+    *reinterpret_cast<uint4*>(img + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    *reinterpret_cast<uint4*>(img + C::A2_BYTES + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+  }
+}
+
+template <int N>
 __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constant__ SweepArgs sa) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
   using T = TcTab<N>;
-  const InvArgs& a = sa.inv;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
   const uint32_t sbase = tc::smem_u32(sm);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::BAR);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::BAR);  // [0] operand load, [1] step 2', [2] step 1'
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::TSLOT);
-  float2* fbuf = reinterpret_cast<float2*>(sm + S::FBUF);
-  float* dcs = reinterpret_cast<float*>(sm + S::DC);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   const int strip = blockIdx.x % sa.strips, seg = blockIdx.x / sa.strips;
@@ -448,7 +555,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
   const int M0 = (int)((long long)seg * nrow / sa.segs);
   const int M1 = (int)((long long)(seg + 1) * nrow / sa.segs);
   const int ncell = min(S::TJ, sa.cells_x - J0);
-  const int ncols = a.g.ncols;
+  auto tile_of = [&](int m) { return sa.img + ((size_t)m * sa.strips + strip) * S::TILE; };
 
   // Constant operands: C2 (hi, lo), then C1 A (hi, lo) and B (hi, lo).
   {
@@ -464,9 +571,13 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    tc::mbar_init(&bar[0], 1);
-    tc::mbar_init(&bar[1], 1);
+    for (int i = 0; i < 3; i++) tc::mbar_init(&bar[i], 1);
     tc::fence_mbar_init();
+    tc::fence_async_smem();
+    if (M0 < M1) {
+      tc::mbar_expect_tx(&bar[0], S::TILE);
+      tc::bulk_load(sm + S::A2, tile_of(M0), S::TILE, &bar[0]);
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -477,60 +588,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
   float* P_new = P_old + S::TJ * S::PC;
 
   for (int m = M0; m < M1; m++) {
-    // F. Temporal filter of the group's bins into shared memory.
-    if (tid < C::G) {
-      const int n = J0 + tid;
-      dcs[tid] = (n <= sa.cells_x && n < ncols) ? block_dc(a, m * ncols + n) : 0.0f;
+    // Step 2' on the tensor cores once the operand tile is in: D2 = A2 * C2^T.
+    if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
+      if (tid == 0) atomicOr(sa.err, 1);
+      break;
     }
-    __syncthreads();
-    {
-      const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
-#pragma unroll 4
-      for (int j = 0; j < C::G * C::PS / kTcThreads; j++) {
-        const int i = tid + kTcThreads * j;
-        const int bl = i / C::PS, li = i - bl * C::PS;
-        const int n = J0 + bl;
-        float2 f = make_float2(0.0f, 0.0f);
-        if (n <= sa.cells_x && n < ncols) f = filter_bin_t<BM, true>(a, dcs[bl], li, gb0 + i);
-        fbuf[bl * S::FS + li] = f;
-      }
-    }
-    __syncthreads();
-
-    // R. Column-inverse operand: row (k', block), K = 2 ky + (re, im).
-    {
-      const int r2 = tid & 127, h = tid >> 7;
-      const int kp = r2 >> 3, bl = r2 & 7;
-      const float2* fb = fbuf + bl * S::FS;
-#pragma unroll
-      for (int cq = 0; cq < C::NY / 4; cq++) {  // 4 ky (one 16-byte chunk) per step
-        uint32_t hi[4], lo[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const int ky = (C::NY) * h + 4 * cq + u;
-          float2 z;
-          if (kp == 0) {
-            const int kym = (N - ky) & (N - 1);
-            const float2 f0 = fb[ky * C::FBW], f0m = fb[kym * C::FBW];
-            const float2 fn = fb[ky * C::FBW + C::NY], fnm = fb[kym * C::FBW + C::NY];
-            const float h0x = 0.5f * (f0.x + f0m.x), h0y = 0.5f * (f0.y - f0m.y);
-            const float hnx = 0.5f * (fn.x + fnm.x), hny = 0.5f * (fn.y - fnm.y);
-            z = make_float2(h0x - hny, h0y + hnx);
-          } else {
-            z = fb[ky * C::FBW + kp];
-          }
-          tc::split_pair(z.x * kInvPre, z.y * kInvPre, hi[u], lo[u]);
-        }
-        const uint32_t o = tc::off_sw128(r2, 2 * (C::NY * h + 4 * cq));
-        *reinterpret_cast<uint4*>(sm + S::A2 + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4*>(sm + S::A2 + C::A2_BYTES + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-      }
-    }
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-
-    // Step 2' on the tensor cores: D2 = A2 * C2^T, three passes.
     if (tid == 0) {
       tc::fence_after_sync();
       constexpr uint32_t id2 = tc::idesc_f16(128, C::N2);
@@ -545,13 +607,18 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
         tc::mma_f16(d, ah, bl, id2, 1);
         tc::mma_f16(d, al, bh, id2, 1);
       }
-      tc::mma_commit(&bar[0]);
+      tc::mma_commit(&bar[1]);
     }
-    if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
+    if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
       if (tid == 0) atomicOr(sa.err, 1);
       break;
     }
     tc::fence_after_sync();
+    // The operand tile is consumed: the next row's starts moving in.
+    if (tid == 0 && m + 1 < M1) {
+      tc::mbar_expect_tx(&bar[0], S::TILE);
+      tc::bulk_load(sm + S::A2, tile_of(m + 1), S::TILE, &bar[0]);
+    }
 
     // V. Row-inverse operand: tile = parity of the block column, row (y, slot).
     {
@@ -595,9 +662,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
           tc::mma_f16(d, al, bh, id1, 1);
         }
       }
-      tc::mma_commit(&bar[1]);
+      tc::mma_commit(&bar[2]);
     }
-    if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
+    if (!__syncthreads_and(tc::mbar_wait(&bar[2], phase, kWaitNs))) {
       if (tid == 0) atomicOr(sa.err, 1);
       break;
     }
@@ -810,30 +877,44 @@ cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st) {
 }
 
 template <int BM>
-cudaError_t launch_sweep_bm(const SweepArgs& a, cudaStream_t st) {
+cudaError_t launch_filter_bm(const SweepArgs& a, int nrow, cudaStream_t st) {
+  constexpr size_t smem = SwpCfg<32>::F_BYTES;
+  auto k = k_filter_tc<32, BM>;
+  cudaError_t e = prepare(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<a.strips * nrow, kTcThreads, smem, st>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st) {
+  if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img) return cudaErrorNotSupported;
+  const int nrow = a.cells_y + 1;
+  cudaError_t e;
+  switch (a.inv.bm) {
+  case -1: e = launch_filter_bm<-1>(a, nrow, st); break;
+  case 1: e = launch_filter_bm<1>(a, nrow, st); break;
+  case 2: e = launch_filter_bm<2>(a, nrow, st); break;
+  case 3: e = launch_filter_bm<3>(a, nrow, st); break;
+  case 4: e = launch_filter_bm<4>(a, nrow, st); break;
+  default: return cudaErrorNotSupported;
+  }
+  if (e != cudaSuccess) return e;
   constexpr size_t smem = SwpCfg<32>::BYTES;
   static_assert(kTcSweepCtasPerSm * (SwpCfg<32>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
   static_assert(SwpCfg<32>::TJ == kTcSweepCells, "cells per strip");
-  auto k = k_sweep_tc<32, BM>;
-  cudaError_t e = prepare(k, smem);
+  e = prepare(k_sweep_tc<32>, smem);
   if (e != cudaSuccess) return e;
-  k<<<a.strips * a.segs, kTcThreads, smem, st>>>(a);
+  k_sweep_tc<32><<<a.strips * a.segs, kTcThreads, smem, st>>>(a);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   return launch_seam_merge(a, st);
 }
 
-cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st) {
-  if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err) return cudaErrorNotSupported;
-  switch (a.inv.bm) {
-  case -1: return launch_sweep_bm<-1>(a, st);
-  case 1: return launch_sweep_bm<1>(a, st);
-  case 2: return launch_sweep_bm<2>(a, st);
-  case 3: return launch_sweep_bm<3>(a, st);
-  case 4: return launch_sweep_bm<4>(a, st);
-  default: return cudaErrorNotSupported;
-  }
+size_t tc_image_bytes(const Geo& g, int strips) {
+  const int cells_y = (g.H + g.bh / 2 - 1) / (g.bh / 2);
+  return (size_t)(cells_y + 1) * strips * SwpCfg<32>::TILE;
 }
 
 }  // namespace f3d

@@ -93,6 +93,7 @@ struct SweepArgs {
   float* seam_t;         // [segs-1][2][bh/2][seam_w]: third and fourth quadrants
   const uint8_t* tab;    // tensor-core form: device copy of tc_tables()
   int* err;              // tensor-core form: set non-zero when a wait gives up
+  uint8_t* img;          // tensor-core form: filtered column-inverse operands, one tile per (row, strip)
 };
 
 // Whether the sweep handles this geometry and form; its CTA grid; the seam
@@ -149,11 +150,13 @@ std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::
                                const std::vector<double>& sxa, const std::vector<double>& sxb,
                                const std::vector<double>& sy);
 cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st);
-// Tensor-core sweep: cells per strip, CTAs per SM, and the launch (with the
-// seam merge of f3d_k_sweep.cu).
+// Tensor-core sweep: cells per strip, CTAs per SM, and the launches (filter,
+// inverse + overlap-add, seam merge of f3d_k_sweep.cu).
 constexpr int kTcSweepCells = 7;
 constexpr int kTcSweepCtasPerSm = 2;
 cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st);
+// Bytes of SweepArgs::img for this geometry and strip count.
+size_t tc_image_bytes(const Geo& g, int strips);
 cudaError_t launch_seam_merge(const SweepArgs& a, cudaStream_t st);
 
 // Counts one kernel launch made by this library (all engines, all threads).
