@@ -77,7 +77,10 @@ struct TcCfg {
 
 constexpr int kTcThreads = 256;
 #ifndef F3D_TC_FILTER_BATCH
-#define F3D_TC_FILTER_BATCH 3
+#define F3D_TC_FILTER_BATCH 1
+#endif
+#ifndef F3D_TC_FILTER_MINB
+#define F3D_TC_FILTER_MINB 5  // filter-kernel CTAs per SM (register budget)
 #endif
 constexpr int kTcFilterBatch = F3D_TC_FILTER_BATCH;  // bins whose loads are in flight together
 constexpr uint64_t kWaitNs = 1000000000ull;  // one second
@@ -380,7 +383,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
 //      Hermitian parts of columns 0 and n/2 as H0 + i H(n/2), scaled by
 //      kInvPre and split hi/lo, written to HBM as the exact shared-memory
 //      image (SWIZZLE_128B) the inverse kernel loads with one bulk copy.
-// With no tensor-memory phases to wait for, it runs at three CTAs per SM.
+// With no tensor-memory phases to wait for, it runs at five CTAs per SM.
 //
 // k_sweep_tc, one CTA per (strip, segment of block rows), per row:
 //   the operand tile arrives by bulk copy (issued while the previous row's
@@ -462,7 +465,7 @@ __device__ __forceinline__ void emit16(const SweepArgs& sa, int y, int x0, const
 }
 
 template <int N, int BM>
-__global__ void __launch_bounds__(kTcThreads, 3) k_filter_tc(const __grid_constant__ SweepArgs sa) {
+__global__ void __launch_bounds__(kTcThreads, F3D_TC_FILTER_MINB) k_filter_tc(const __grid_constant__ SweepArgs sa) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
   const InvArgs& a = sa.inv;
