@@ -283,8 +283,7 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
     sa.err = e->d_err;
     sa.img = e->d_img;
     cudaEventRecord(e->ev[2], e->stream);
-    cudaError_t ce = launch_sweep(e->inv_form, sa, e->stream);
-    cudaEventRecord(e->ev[4], e->stream);
+    cudaError_t ce = launch_sweep(e->inv_form, sa, e->stream, e->ev[4]);
     cudaEventRecord(e->ev[3], e->stream);
     e->proc_timed = true;
     if (ce != cudaSuccess) return e->cuda_fail(ce, "the fused filter/inverse/overlap-add launch");

@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256) k_seam_merge(const __grid_constant__ Swee
 }
 
 template <int BW, int BH, int BM>
-cudaError_t launch_bm(const SweepArgs& a, cudaStream_t st) {
+cudaError_t launch_bm(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
   using S_ = SCfg<BW, BH>;
   auto k = k_sweep_fast<BW, BH, BM>;
   static_assert(S_::SMEM * F3D_SWEEP_MINB <= 227 * 1024, "CTAs per SM");
@@ -182,17 +182,18 @@ cudaError_t launch_bm(const SweepArgs& a, cudaStream_t st) {
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  if (mark) cudaEventRecord(mark, st);
   return launch_seam_merge(a, st);
 }
 
 template <int BW, int BH>
-cudaError_t launch_size(const SweepArgs& a, cudaStream_t st) {
+cudaError_t launch_size(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
   switch (a.inv.bm) {
-  case -1: return launch_bm<BW, BH, -1>(a, st);
-  case 1: return launch_bm<BW, BH, 1>(a, st);
-  case 2: return launch_bm<BW, BH, 2>(a, st);
-  case 3: return launch_bm<BW, BH, 3>(a, st);
-  case 4: return launch_bm<BW, BH, 4>(a, st);
+  case -1: return launch_bm<BW, BH, -1>(a, st, mark);
+  case 1: return launch_bm<BW, BH, 1>(a, st, mark);
+  case 2: return launch_bm<BW, BH, 2>(a, st, mark);
+  case 3: return launch_bm<BW, BH, 3>(a, st, mark);
+  case 4: return launch_bm<BW, BH, 4>(a, st, mark);
   default: return cudaErrorNotSupported;
   }
 }
@@ -236,13 +237,13 @@ size_t sweep_seam_floats(const Geo& g, int segs) {
   return (size_t)(segs > 1 ? segs - 1 : 0) * 3 * (g.bh / 2) * (size_t)cells_x * (g.bw / 2);
 }
 
-cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st) {
+cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
   if (!sweep_supported(form, a.inv.g, a.inv.bm)) return cudaErrorNotSupported;
-  if (form == F3D_FORM_TC) return launch_sweep_tc(a, st);
+  if (form == F3D_FORM_TC) return launch_sweep_tc(a, st, mark);
   switch (a.inv.g.bw) {
-  case 8: return launch_size<8, 8>(a, st);
-  case 16: return launch_size<16, 16>(a, st);
-  case 32: return launch_size<32, 32>(a, st);
+  case 8: return launch_size<8, 8>(a, st, mark);
+  case 16: return launch_size<16, 16>(a, st, mark);
+  case 32: return launch_size<32, 32>(a, st, mark);
   default: return cudaErrorNotSupported;
   }
 }

@@ -890,7 +890,7 @@ cudaError_t launch_filter_bm(const SweepArgs& a, int nrow, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st) {
+cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
   if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img) return cudaErrorNotSupported;
   const int nrow = a.cells_y + 1;
   cudaError_t e;
@@ -903,6 +903,7 @@ cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st) {
   default: return cudaErrorNotSupported;
   }
   if (e != cudaSuccess) return e;
+  if (mark) cudaEventRecord(mark, st);
   constexpr size_t smem = SwpCfg<32>::BYTES;
   static_assert(kTcSweepCtasPerSm * (SwpCfg<32>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
   static_assert(SwpCfg<32>::TJ == kTcSweepCells, "cells per strip");

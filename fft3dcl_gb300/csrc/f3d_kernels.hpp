@@ -101,7 +101,9 @@ struct SweepArgs {
 bool sweep_supported(int form, const Geo& g, int bm);
 void sweep_plan(int form, const Geo& g, int sm_count, int* strips, int* segs);
 size_t sweep_seam_floats(const Geo& g, int segs);
-cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st);
+// `mark` (optional) is recorded after the first kernel: the fast-form sweep,
+// or the tensor-core filter kernel.
+cudaError_t launch_sweep(int form, const SweepArgs& a, cudaStream_t st, cudaEvent_t mark = nullptr);
 
 // Kernel launches; each returns the launch error. `form` is F3D_FORM_*.
 cudaError_t launch_forward(int form, const FwdArgs& a, cudaStream_t st);
@@ -154,7 +156,7 @@ cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st);
 // inverse + overlap-add, seam merge of f3d_k_sweep.cu).
 constexpr int kTcSweepCells = 7;
 constexpr int kTcSweepCtasPerSm = 2;
-cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st);
+cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark);
 // Bytes of SweepArgs::img for this geometry and strip count.
 size_t tc_image_bytes(const Geo& g, int strips);
 cudaError_t launch_seam_merge(const SweepArgs& a, cudaStream_t st);

@@ -187,9 +187,13 @@ int f3d_prune(f3d_engine* e, int lo, int hi);
 
 /* Wait for all queued work of the engine. */
 int f3d_synchronize(f3d_engine* e);
-/* Device time of the kernels of the last forward / process calls in ms:
- * ms[0] forward transform, ms[1] filter + inverse, ms[2] overlap-add + pack
- * (CUDA events on the engine stream; valid after f3d_synchronize). */
+/* Device time of the kernels of the last forward / process calls in ms
+ * (CUDA events on the engine stream; valid after f3d_synchronize):
+ * ms[0] forward transform;
+ * ms[1] filter + inverse (separate kernels), the whole sweep (fused fast
+ *       form) or the filter kernel (tensor-core form);
+ * ms[2] overlap-add + pack (separate kernels), the seam merge (fused fast
+ *       form) or inverse + overlap-add + seam merge (tensor-core form). */
 int f3d_last_kernel_ms(f3d_engine* e, float* ms);
 
 /* GpuRef::liveInstances / liveBytes (src/cl/gpu.cpp:44-57). */
