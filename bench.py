@@ -352,6 +352,24 @@ def run_gpu(args, rank, world, local_rank):
                 "d2h_bytes_per_step": W * H * 2},
         "gpu_launches": int(launches), "clocks": clk,
     }
+    if world == 1 and args.serve_streams > 0:
+        # The serving workload: mixed streams with Poisson frame arrivals,
+        # through the serving loop (continuous batching, HBM-budget admission).
+        from fft3dcl_gb300 import serving
+        specs = serving.mixed_streams(args.serve_streams, args.serve_frames)
+        sframes = [serving.stream_frames(s, distinct=4) for s in specs]
+        with F.Server(form=args.form, device=local_rank, max_streams=args.serve_streams,
+                      hbm_budget=200 << 30) as sv:
+            _, st = serving.run(sv, specs, sframes, realtime=True, timeout_s=300)
+        line["serving"] = {
+            "streams": len(specs), "frames_per_stream": args.serve_frames,
+            "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3), "max_ms": round(st["max_ms"], 3),
+            "frames_per_s": round(st["frames"] / st["seconds"], 1) if st["seconds"] > 0 else None,
+            "offered_frames_per_s": round(sum(s["fps"] for s in specs), 1),
+            "mix": "resolutions 640x360..3840x2160, 8/10-bit luma, bt in {1,3,4}, bw in {16,32} (bw 16 runs the fast form)",
+            "arrivals": "Poisson, 24-60 frames/s per stream",
+            "latency": "arrival of the last input frame an output's window needs -> output copied to host memory",
+            "form": args.form}
     if world == 1 and not args.no_cpu:
         cpu_threads = os.cpu_count() or 1
         fps_cpu, steps = cpu_steady_state(frames, cpu_threads, 12.0, 30)
@@ -375,6 +393,8 @@ def main():
     ap.add_argument("--compare", default="exact,fast",
                     help="comma-separated forms whose device throughput is reported under 'forms'")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--serve-streams", type=int, default=16, help="streams of the serving run (0: skip it)")
+    ap.add_argument("--serve-frames", type=int, default=120, help="frames per serving stream")
     ap.add_argument("--frames", type=int, default=NFRAMES,
                     help="frames of the resident clip (fewer only to keep profiler captures small)")
     args = ap.parse_args()

@@ -98,6 +98,8 @@ EXPORTS = (
     "f3d_bytes_per_sample", "f3d_upload_degrid_sample", "f3d_process", "f3d_process_raw",
     "f3d_process_device", "f3d_prune", "f3d_synchronize", "f3d_last_kernel_ms",
     "f3d_live_instances", "f3d_live_bytes", "f3d_kernel_launches", "f3d_denoise_noalloc",
+    "f3d_server_create", "f3d_server_destroy", "f3d_server_open", "f3d_server_submit", "f3d_server_poll",
+    "f3d_server_close", "f3d_server_get_stats",
 )
 
 _lib = None
@@ -136,6 +138,14 @@ def lib():
         L.f3d_process.argtypes = [vp, P(i), i, vp]
         L.f3d_process_raw.argtypes = [vp, P(i), i, vp, sz]
         L.f3d_process_device.argtypes = [vp, P(i), i, vp, sz]
+        L.f3d_server_create.argtypes = [P(ServerConfig), P(vp)]
+        L.f3d_server_destroy.argtypes = [vp]
+        L.f3d_server_destroy.restype = None
+        L.f3d_server_open.argtypes = [vp, P(ScriptParams), P(PlaneGeom), i, P(i)]
+        L.f3d_server_submit.argtypes = [vp, i, i, vp, C.c_longlong]
+        L.f3d_server_poll.argtypes = [vp, i, P(i), vp, C.c_longlong, i]
+        L.f3d_server_close.argtypes = [vp, i]
+        L.f3d_server_get_stats.argtypes = [vp, P(ServerStats)]
         L.f3d_prune.argtypes = [vp, i, i]
         L.f3d_synchronize.argtypes = [vp]
         L.f3d_last_kernel_ms.argtypes = [vp, P(C.c_float)]
@@ -144,6 +154,19 @@ def lib():
         L.f3d_kernel_launches.restype = C.c_uint64
         _lib = L
     return _lib
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("form", C.c_int), ("max_streams", C.c_int), ("hbm_budget", C.c_size_t)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("frames", C.c_longlong), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("max_ms", C.c_double), ("mean_ms", C.c_double), ("seconds", C.c_double),
+                ("open_streams", C.c_int), ("used_bytes", C.c_size_t)]
+
+
+F3D_E_BUSY = -6
 
 
 class F3DError(RuntimeError):
@@ -467,3 +490,81 @@ def FFT3DCL(clip, fmt: VideoFormat | None = None, **params):
     finally:
         flt.close()
     return [r[0] for r in res] if single else res
+
+
+class Server:
+    """The serving loop (f3d_server_*): many plane streams of any size, depth
+    and parameters on one GPU, admitted by an HBM budget, each keeping its
+    window spectra resident, launched concurrently as their frames arrive."""
+
+    def __init__(self, form: str = "tc", device: int = 0, max_streams: int = 16,
+                 hbm_budget: int = 64 << 30):
+        cfg = ServerConfig(device, FORMS[form], max_streams, hbm_budget)
+        h = C.c_void_p()
+        if lib().f3d_server_create(C.byref(cfg), C.byref(h)) != F3D_OK:
+            raise F3DError(lib().f3d_last_error().decode())
+        self._h = h
+        self._geom = {}
+
+    @staticmethod
+    def _rc(rc):
+        if rc == F3D_E_BUSY:
+            return False
+        if rc != F3D_OK:
+            raise F3DError(lib().f3d_last_error().decode())
+        return True
+
+    def open(self, width: int, height: int, bits: int, nframes: int, sample_type: int = 0,
+             chroma: bool = False, **params):
+        """Stream id, or None when the server has no slot or budget for it now."""
+        sp = script_params(**params)
+        geom = PlaneGeom(width, height, bits, sample_type, int(chroma))
+        sid = C.c_int(-1)
+        if not self._rc(lib().f3d_server_open(self._h, C.byref(sp), C.byref(geom), nframes, C.byref(sid))):
+            return None
+        dtype = np.float32 if sample_type == 1 else (np.uint8 if bits <= 8 else np.uint16)
+        self._geom[sid.value] = (width, height, dtype)
+        return sid.value
+
+    def submit(self, sid: int, n: int, frame: np.ndarray) -> bool:
+        """Queues frame n; False when the stream's input slots are full."""
+        f = np.ascontiguousarray(frame)
+        return self._rc(lib().f3d_server_submit(self._h, sid, n, f.ctypes.data_as(C.c_void_p), f.strides[0]))
+
+    def poll(self, sid: int, timeout_ms: int = 0):
+        """(frame number, output plane) of the stream's next finished output,
+        or None."""
+        w, h, dtype = self._geom[sid]
+        out = np.empty((h, w), dtype)
+        n = C.c_int(-1)
+        if not self._rc(lib().f3d_server_poll(self._h, sid, C.byref(n), out.ctypes.data_as(C.c_void_p),
+                                              out.strides[0], timeout_ms)):
+            return None
+        return n.value, out
+
+    def close_stream(self, sid: int):
+        self._rc(lib().f3d_server_close(self._h, sid))
+        self._geom.pop(sid, None)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self._rc(lib().f3d_server_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().f3d_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -477,8 +477,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
       return finish_fail(e->cuda_fail(ce, "tensor-core table upload"));
   }
   if ((ce = e->alloc(&e->d_in, plane_bytes)) != cudaSuccess ||
-      (ce = e->alloc(&e->d_out, plane_bytes)) != cudaSuccess ||
-      (ce = e->alloc(&e->d_blocks, sizeof(float) * bwbh * e->grid.nb)) != cudaSuccess)
+      (ce = e->alloc(&e->d_out, plane_bytes)) != cudaSuccess)
     return finish_fail(e->cuda_fail(ce, "buffer allocation"));
   if (ip.bm == 0) {
     const size_t nbin = (size_t)e->grid.nb * e->ps;
@@ -504,6 +503,9 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
     const int fl = opts ? opts->flags : 0;
     e->sweep_prefetch = (fl & F3D_FLAG_PREFETCH_EARLY) ? 1 : (fl & F3D_FLAG_PREFETCH_LATE) ? 2 : 0;
   }
+  // The windowed-block buffer of the separate inverse and overlap-add kernels.
+  if (!e->fused && (ce = e->alloc(&e->d_blocks, sizeof(float) * bwbh * e->grid.nb)) != cudaSuccess)
+    return finish_fail(e->cuda_fail(ce, "buffer allocation"));
   *out = e;
   return F3D_OK;
 }

@@ -1,0 +1,408 @@
+// f3d_serve.cpp -- the serving loop: concurrent streams of planes of any
+// size, bit depth and parameters on one GPU.
+//
+// The reference serves one clip per filter instance and lets VapourSynth call
+// getFrame from many threads, serialised per instance by a mutex
+// (src/fft3dcl.cpp:289, :365-368). Here one server owns the GPU work of many
+// streams:
+//  - admission: a stream is opened only while the device memory of all open
+//    streams (engine tables and buffers, its window's spectra cache, its
+//    staging planes) fits the server's HBM budget and a slot is free;
+//    otherwise f3d_server_open answers F3D_E_BUSY and the caller retries once
+//    another stream has closed;
+//  - residency: each stream has its own engine, so its temporal-window
+//    spectra (and Kalman state) stay in HBM between frames;
+//  - continuous batching: one scheduler thread launches, on every pass, the
+//    next output of every stream whose window frames have arrived, each
+//    stream on its own CUDA stream, so the kernels of different streams run
+//    concurrently; streams opened while others run join the next pass;
+//  - latency: an output's latency runs from the arrival of the last input
+//    frame its window needs to the completion of its readback to host memory.
+#include "fft3d_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace f3d {
+void set_last_error(const char* msg);
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(Clock::now().time_since_epoch()).count();
+}
+
+int fail(int code, const std::string& msg) {
+  static thread_local std::string m;
+  m = msg;
+  f3d::set_last_error(m.c_str());
+  return code;
+}
+
+constexpr int kInSlots = 6;   // submitted frames a stream may hold before they are uploaded
+constexpr int kOutSlots = 3;  // outputs a stream may hold before they are polled
+
+struct InSlot {
+  uint8_t* host = nullptr;  // pinned
+  int frame = -1;
+  enum { FREE, FULL, UPLOADED } state = FREE;
+  long long seq = 0;        // output launch count when the upload was queued
+  double t_arrive = 0.0;
+};
+
+struct OutSlot {
+  uint8_t* host = nullptr;  // pinned
+  cudaEvent_t ev = nullptr;
+  int frame = -1;
+  long long seq = 0;
+  double t_ready = 0.0, t_done = 0.0;
+  bool busy = false, done = false;
+};
+
+struct Stream {
+  int id = -1;
+  f3d_engine* eng = nullptr;
+  cudaStream_t cs = nullptr;
+  int W = 0, H = 0, bps = 1, nframes = 0, need = 1, cur = 0, bt = 1;
+  size_t row_bytes = 0, plane_bytes = 0, est_bytes = 0;
+  uint8_t* d_src = nullptr;
+  uint8_t* d_dst = nullptr;
+  InSlot in[kInSlots];
+  std::deque<OutSlot*> outs;  // launched, in frame order
+  OutSlot out_pool[kOutSlots];
+  int next_out = 0;           // next output frame to launch
+  long long seq = 0;
+  std::vector<double> arrive; // arrival time of each input frame
+  bool closing = false;
+  std::string err;
+};
+
+void free_stream(Stream* s) {
+  if (s->cs) cudaStreamSynchronize(s->cs);
+  if (s->eng) f3d_engine_destroy(s->eng);
+  for (auto& i : s->in)
+    if (i.host) cudaFreeHost(i.host);
+  for (auto& o : s->out_pool) {
+    if (o.host) cudaFreeHost(o.host);
+    if (o.ev) cudaEventDestroy(o.ev);
+  }
+  if (s->d_src) cudaFree(s->d_src);
+  if (s->d_dst) cudaFree(s->d_dst);
+  if (s->cs) cudaStreamDestroy(s->cs);
+  delete s;
+}
+
+}  // namespace
+
+struct f3d_server {
+  f3d_server_config cfg{};
+  std::mutex mtx;
+  std::condition_variable work_cv, done_cv;
+  std::map<int, Stream*> streams;
+  int next_id = 0;
+  size_t used_bytes = 0;
+  std::vector<double> lat;  // per-output latency, ms
+  double t_first = -1.0, t_last = 0.0;
+  std::atomic<bool> stop{false};
+  std::thread worker;
+
+  void run();
+  bool ready(Stream* s, int n, std::vector<int>& win);
+  void launch(Stream* s, int n, const std::vector<int>& win);
+  void reap(Stream* s);
+};
+
+// Window of output n (src/fft3dcl.cpp:396-430): frames clamp(n - cur + i).
+bool f3d_server::ready(Stream* s, int n, std::vector<int>& win) {
+  win.clear();
+  for (int i = 0; i < s->need; i++) win.push_back(std::min(std::max(n - s->cur + i, 0), s->nframes - 1));
+  for (int fn : win) {
+    if (f3d_has(s->eng, fn)) continue;
+    bool found = false;
+    for (auto& slot : s->in)
+      if (slot.state == InSlot::FULL && slot.frame == fn) found = true;
+    if (!found) return false;
+  }
+  return true;
+}
+
+void f3d_server::launch(Stream* s, int n, const std::vector<int>& win) {
+  OutSlot* o = nullptr;
+  for (auto& c : s->out_pool)
+    if (!c.busy) {
+      o = &c;
+      break;
+    }
+  double t_ready = 0.0;
+  int rc = F3D_OK;
+  for (int fn : win) {
+    t_ready = std::max(t_ready, s->arrive[fn]);
+    if (f3d_has(s->eng, fn)) continue;
+    for (auto& slot : s->in) {
+      if (slot.state != InSlot::FULL || slot.frame != fn) continue;
+      cudaMemcpyAsync(s->d_src, slot.host, s->plane_bytes, cudaMemcpyHostToDevice, s->cs);
+      if (rc == F3D_OK) rc = f3d_forward_device(s->eng, fn, s->d_src, s->row_bytes);
+      slot.state = InSlot::UPLOADED;
+      slot.seq = s->seq;
+      break;
+    }
+  }
+  if (rc == F3D_OK) rc = f3d_process_device(s->eng, win.data(), (int)win.size(), s->d_dst, s->row_bytes);
+  if (rc != F3D_OK && s->err.empty()) s->err = f3d_engine_error(s->eng);
+  cudaMemcpyAsync(o->host, s->d_dst, s->plane_bytes, cudaMemcpyDeviceToHost, s->cs);
+  cudaEventRecord(o->ev, s->cs);
+  // The plugin's cache window (src/fft3dcl.cpp:457-466).
+  f3d_prune(s->eng, n - s->cur - 1, n - s->cur + s->bt);
+  o->busy = true;
+  o->done = false;
+  o->frame = n;
+  o->seq = s->seq++;
+  o->t_ready = t_ready;
+  s->outs.push_back(o);
+}
+
+// Marks finished outputs done and frees the input slots their uploads used.
+void f3d_server::reap(Stream* s) {
+  for (OutSlot* o : s->outs) {
+    if (o->done) continue;
+    if (cudaEventQuery(o->ev) != cudaSuccess) break;  // outputs finish in order on one stream
+    o->done = true;
+    o->t_done = now_ms();
+    lat.push_back(o->t_done - o->t_ready);
+    if (t_first < 0.0) t_first = o->t_ready;
+    t_last = std::max(t_last, o->t_done);
+    for (auto& slot : s->in)
+      if (slot.state == InSlot::UPLOADED && slot.seq <= o->seq) slot.state = InSlot::FREE;
+  }
+}
+
+void f3d_server::run() {
+  cudaSetDevice(cfg.device);
+  std::vector<int> win;
+  std::unique_lock<std::mutex> lk(mtx);
+  while (!stop) {
+    bool any = false, pending = false;
+    for (auto& kv : streams) {
+      Stream* s = kv.second;
+      reap(s);
+      if (s->closing) continue;
+      // Continuous batching: every stream whose next window is complete
+      // gets its output launched in this pass.
+      while (s->next_out < s->nframes && (int)s->outs.size() < kOutSlots && ready(s, s->next_out, win)) {
+        launch(s, s->next_out, win);
+        s->next_out++;
+        any = true;
+      }
+      for (OutSlot* o : s->outs) pending |= !o->done;
+    }
+    done_cv.notify_all();
+    if (!any) {
+      // In-flight outputs are polled every 50 us; otherwise sleep until a
+      // frame or a stream arrives.
+      if (pending) work_cv.wait_for(lk, std::chrono::microseconds(50));
+      else work_cv.wait_for(lk, std::chrono::milliseconds(5));
+    }
+  }
+}
+
+extern "C" {
+
+int f3d_server_create(const f3d_server_config* cfg, f3d_server** out) {
+  if (!cfg || !out) return fail(F3D_E_PARAM, "FFT3DCL: null argument");
+  *out = nullptr;
+  if (cfg->max_streams <= 0 || cfg->hbm_budget == 0) return fail(F3D_E_PARAM, "FFT3DCL: empty server budget");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return fail(F3D_E_CUDA, "FFT3DCL: no CUDA device available");
+  }
+  if (cfg->device < 0 || cfg->device >= ndev) return fail(F3D_E_PARAM, "FFT3DCL: device ordinal out of range");
+  auto* sv = new f3d_server();
+  sv->cfg = *cfg;
+  sv->worker = std::thread([sv] { sv->run(); });
+  *out = sv;
+  return F3D_OK;
+}
+
+void f3d_server_destroy(f3d_server* sv) {
+  if (!sv) return;
+  sv->stop = true;
+  sv->work_cv.notify_all();
+  if (sv->worker.joinable()) sv->worker.join();
+  cudaSetDevice(sv->cfg.device);
+  for (auto& kv : sv->streams) free_stream(kv.second);
+  delete sv;
+}
+
+int f3d_server_open(f3d_server* sv, const f3d_script_params* sp, const f3d_plane_geom* geom, int nframes,
+                    int* sid) {
+  if (!sv || !sp || !geom || !sid || nframes <= 0) return fail(F3D_E_PARAM, "FFT3DCL: bad stream arguments");
+  cudaSetDevice(sv->cfg.device);
+  {
+    std::lock_guard<std::mutex> lk(sv->mtx);
+    if ((int)sv->streams.size() >= sv->cfg.max_streams) return fail(F3D_E_BUSY, "FFT3DCL: no free stream slot");
+  }
+  auto s = std::unique_ptr<Stream, void (*)(Stream*)>(new Stream(), free_stream);
+  if (cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(F3D_E_CUDA, "FFT3DCL: stream creation failed");
+  f3d_options o{sv->cfg.device, sv->cfg.form, s->cs, 0};
+  int rc = f3d_engine_create(sp, geom, &o, &s->eng);
+  if (rc != F3D_OK) return rc;
+  f3d_engine_info info{};
+  f3d_engine_get_info(s->eng, &info);
+  s->W = geom->width;
+  s->H = geom->height;
+  s->bps = info.bytes_per_sample;
+  s->row_bytes = (size_t)s->W * s->bps;
+  s->plane_bytes = s->row_bytes * s->H;
+  s->nframes = nframes;
+  s->arrive.assign(nframes, 0.0);
+  f3d_internal_params ip{};
+  f3d_validate_params(sp, geom->width, geom->height, geom->bits, &ip);
+  s->bt = ip.bt;
+  s->need = ip.bm >= 2 ? ip.bt : 1;
+  s->cur = ip.bm >= 2 ? ip.current : 0;
+  // Steady state: the engine's own buffers, a cache of bt + 2 window spectra
+  // plus one retired spectrum awaiting reuse, and the two staging planes.
+  s->est_bytes = info.device_bytes + (size_t)(s->bt + 3) * info.spectrum_bytes + 2 * s->plane_bytes;
+  {
+    std::lock_guard<std::mutex> lk(sv->mtx);
+    if (sv->used_bytes + s->est_bytes > sv->cfg.hbm_budget)
+      return fail(F3D_E_BUSY, "FFT3DCL: the stream does not fit the server's HBM budget now");
+    sv->used_bytes += s->est_bytes;
+  }
+  bool ok = cudaMalloc(&s->d_src, s->plane_bytes) == cudaSuccess && cudaMalloc(&s->d_dst, s->plane_bytes) == cudaSuccess;
+  for (auto& i : s->in) ok = ok && cudaMallocHost(&i.host, s->plane_bytes) == cudaSuccess;
+  for (auto& c : s->out_pool)
+    ok = ok && cudaMallocHost(&c.host, s->plane_bytes) == cudaSuccess &&
+         cudaEventCreateWithFlags(&c.ev, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    std::lock_guard<std::mutex> lk(sv->mtx);
+    sv->used_bytes -= s->est_bytes;
+    return fail(F3D_E_NOMEM, "FFT3DCL: stream buffers could not be allocated");
+  }
+  std::lock_guard<std::mutex> lk(sv->mtx);
+  Stream* st = s.release();
+  st->id = sv->next_id++;
+  *sid = st->id;
+  sv->streams[st->id] = st;
+  sv->work_cv.notify_all();
+  return F3D_OK;
+}
+
+int f3d_server_submit(f3d_server* sv, int sid, int n, const void* src, long long pitch) {
+  if (!sv || !src) return fail(F3D_E_PARAM, "FFT3DCL: null argument");
+  Stream* s;
+  InSlot* slot = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(sv->mtx);
+    auto it = sv->streams.find(sid);
+    if (it == sv->streams.end()) return fail(F3D_E_PARAM, "FFT3DCL: unknown stream");
+    s = it->second;
+    if (n < 0 || n >= s->nframes) return fail(F3D_E_PARAM, "FFT3DCL: frame number out of range");
+    if (pitch < (long long)s->row_bytes) return fail(F3D_E_PARAM, "FFT3DCL: pitch too small");
+    for (auto& i : s->in)
+      if (i.state == InSlot::FREE) {
+        slot = &i;
+        break;
+      }
+    if (!slot) return fail(F3D_E_BUSY, "FFT3DCL: the stream's input slots are full");
+    slot->state = InSlot::UPLOADED;  // reserved while the copy below runs
+    slot->frame = -1;
+    slot->seq = -1;
+  }
+  const uint8_t* p = static_cast<const uint8_t*>(src);
+  for (int y = 0; y < s->H; y++) std::memcpy(slot->host + y * s->row_bytes, p + y * pitch, s->row_bytes);
+  {
+    std::lock_guard<std::mutex> lk(sv->mtx);
+    slot->frame = n;
+    slot->t_arrive = now_ms();
+    s->arrive[n] = slot->t_arrive;
+    slot->state = InSlot::FULL;
+  }
+  sv->work_cv.notify_all();
+  return F3D_OK;
+}
+
+int f3d_server_poll(f3d_server* sv, int sid, int* n, void* dst, long long pitch, int timeout_ms) {
+  if (!sv || !n) return fail(F3D_E_PARAM, "FFT3DCL: null argument");
+  std::unique_lock<std::mutex> lk(sv->mtx);
+  auto it = sv->streams.find(sid);
+  if (it == sv->streams.end()) return fail(F3D_E_PARAM, "FFT3DCL: unknown stream");
+  Stream* s = it->second;
+  auto front_done = [&] { return !s->outs.empty() && s->outs.front()->done; };
+  if (!sv->done_cv.wait_for(lk, std::chrono::milliseconds(std::max(timeout_ms, 0)), front_done))
+    return fail(F3D_E_BUSY, "FFT3DCL: no finished output yet");
+  OutSlot* o = s->outs.front();
+  if (!s->err.empty()) return fail(F3D_E_CUDA, s->err);
+  if (dst && pitch < (long long)s->row_bytes) return fail(F3D_E_PARAM, "FFT3DCL: pitch too small");
+  *n = o->frame;
+  // The copy runs without the server lock, so that the scheduler keeps
+  // launching meanwhile; the slot stays busy (not reused) until it is done.
+  // One thread polls a stream.
+  lk.unlock();
+  if (dst) {
+    uint8_t* d = static_cast<uint8_t*>(dst);
+    for (int y = 0; y < s->H; y++) std::memcpy(d + y * pitch, o->host + y * s->row_bytes, s->row_bytes);
+  }
+  lk.lock();
+  s->outs.pop_front();
+  o->busy = false;
+  sv->work_cv.notify_all();
+  return F3D_OK;
+}
+
+int f3d_server_close(f3d_server* sv, int sid) {
+  if (!sv) return fail(F3D_E_PARAM, "FFT3DCL: null argument");
+  Stream* s;
+  {
+    std::lock_guard<std::mutex> lk(sv->mtx);
+    auto it = sv->streams.find(sid);
+    if (it == sv->streams.end()) return fail(F3D_E_PARAM, "FFT3DCL: unknown stream");
+    s = it->second;
+    sv->streams.erase(it);
+    sv->used_bytes -= s->est_bytes;
+  }
+  free_stream(s);
+  sv->work_cv.notify_all();
+  return F3D_OK;
+}
+
+int f3d_server_get_stats(f3d_server* sv, f3d_server_stats* st) {
+  if (!sv || !st) return fail(F3D_E_PARAM, "FFT3DCL: null argument");
+  std::lock_guard<std::mutex> lk(sv->mtx);
+  std::vector<double> v = sv->lat;
+  std::memset(st, 0, sizeof *st);
+  st->frames = (long long)v.size();
+  st->open_streams = (int)sv->streams.size();
+  st->used_bytes = sv->used_bytes;
+  if (v.empty()) return F3D_OK;
+  std::sort(v.begin(), v.end());
+  auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * (v.size() - 1) + 0.5))]; };
+  st->p50_ms = pct(0.50);
+  st->p99_ms = pct(0.99);
+  st->max_ms = v.back();
+  double sum = 0.0;
+  for (double x : v) sum += x;
+  st->mean_ms = sum / v.size();
+  st->seconds = (sv->t_last - sv->t_first) / 1000.0;
+  return F3D_OK;
+}
+
+}  // extern "C"

@@ -39,7 +39,8 @@ enum {
   F3D_E_CUDA = -2,      /* a CUDA call failed (message has the reason)    */
   F3D_E_NOMEM = -3,     /* device allocation failed                       */
   F3D_E_STATE = -4,     /* call out of order (missing spectra, ...)       */
-  F3D_E_UNSUPPORTED = -5 /* feature not available on this path           */
+  F3D_E_UNSUPPORTED = -5, /* feature not available on this path          */
+  F3D_E_BUSY = -6         /* no capacity now (server slot, budget, queue); retry later */
 };
 
 /* Script-level parameters: names, types and defaults of ScriptParams,
@@ -230,6 +231,54 @@ uint64_t f3d_kernel_launches(void);
 int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
                         const void* const* dev_window, int nwin, size_t src_pitch, void* dev_dst,
                         size_t dst_pitch, void* stream);
+
+/* ---- Serving loop ----------------------------------------------------------
+ * Replaces the reference's one-instance-per-clip model (src/fft3dcl.cpp:289,
+ * :365-368: VapourSynth requests serialised per instance by a mutex) for
+ * hosts that serve many streams at once. A server owns one GPU and one
+ * scheduler thread. Each stream is one plane sequence with its own
+ * parameters, size and format, and its own engine (window spectra and Kalman
+ * state stay in HBM). Streams are admitted while the device memory of all open
+ * streams fits `hbm_budget` and fewer than `max_streams` are open; otherwise
+ * f3d_server_open returns F3D_E_BUSY. On every pass the scheduler launches
+ * the next output of every stream whose window frames have arrived, each
+ * stream on its own CUDA stream, so streams' kernels overlap on the device
+ * and streams that open while others run join at once. Latency of an output:
+ * from the arrival of the last input frame its window needs to the end of
+ * its copy to host memory. */
+typedef struct {
+  int device;
+  int form;          /* F3D_FORM_* for every stream (per-stream fallbacks as in create) */
+  int max_streams;
+  size_t hbm_budget; /* bytes of device memory the open streams may hold */
+} f3d_server_config;
+
+typedef struct {
+  long long frames;  /* outputs finished */
+  double p50_ms, p99_ms, max_ms, mean_ms;
+  double seconds;    /* first input ready to last output done */
+  int open_streams;
+  size_t used_bytes; /* admitted device memory */
+} f3d_server_stats;
+
+typedef struct f3d_server f3d_server;
+
+int f3d_server_create(const f3d_server_config* cfg, f3d_server** out);
+void f3d_server_destroy(f3d_server* sv);
+/* Opens a stream of `nframes` frames (window clamping at both ends as in the
+ * plugin, src/fft3dcl.cpp:303-331); *sid receives its id. */
+int f3d_server_open(f3d_server* sv, const f3d_script_params* sp, const f3d_plane_geom* geom, int nframes,
+                    int* sid);
+/* Frame n (submit in frame order) from host memory; copied before return.
+ * F3D_E_BUSY when the stream holds its maximum of frames not yet uploaded. */
+int f3d_server_submit(f3d_server* sv, int sid, int n, const void* src, long long pitch);
+/* Next finished output of the stream in frame order, waiting up to
+ * timeout_ms; *n receives its frame number and dst (if not NULL) its samples.
+ * F3D_E_BUSY when none finished in time. One thread polls a given stream. */
+int f3d_server_poll(f3d_server* sv, int sid, int* n, void* dst, long long pitch, int timeout_ms);
+/* Releases the stream and its share of the budget. */
+int f3d_server_close(f3d_server* sv, int sid);
+int f3d_server_get_stats(f3d_server* sv, f3d_server_stats* st);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,70 @@
+"""The serving loop: streams of different sizes, depths and parameters run
+concurrently, each result is the same as the stream run alone (bit for bit:
+the same kernels on the same inputs), admission follows the HBM budget and
+slots, and latency figures are reported."""
+import numpy as np
+import pytest
+
+import fft3dcl_gb300 as F
+from fft3dcl_gb300 import serving, synth
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [
+    dict(width=640, height=360, bits=8, frames=9, fps=60.0, seed=11, params=dict(bt=3)),
+    dict(width=1280, height=720, bits=10, frames=7, fps=40.0, seed=12, params=dict(bt=4, sharpen=0.3)),
+    dict(width=333, height=177, bits=8, frames=6, fps=50.0, seed=13, params=dict(bt=1, bw=16, bh=16)),
+    dict(width=960, height=540, bits=10, frames=8, fps=30.0, seed=14, params=dict(bt=2, bw=32, bh=32)),
+    dict(width=320, height=240, bits=8, frames=10, fps=45.0, seed=15, params=dict(bt=0, sigma=2.0)),
+]
+
+
+def alone(spec, frames, form):
+    bits = spec["bits"]
+    seq = [frames[n % len(frames)] for n in range(spec["frames"])]
+    flt = F.Filter([[f] for f in seq], F.VideoFormat("gray", bits, 0), form=form, **spec["params"])
+    try:
+        return [flt.get_frame(n)[0] for n in range(spec["frames"])]
+    finally:
+        flt.close()
+
+
+@pytest.mark.parametrize("form", ["tc", "fast"])
+def test_mixed_streams_equal_alone(form):
+    frames = [serving.stream_frames(s, distinct=4) for s in SPECS]
+    with F.Server(form=form, max_streams=8) as sv:
+        outs, st = serving.run(sv, SPECS, frames, realtime=True, timeout_s=120)
+    assert st["frames"] == sum(s["frames"] for s in SPECS)
+    assert st["p99_ms"] >= st["p50_ms"] > 0.0
+    for spec, fr, got in zip(SPECS, frames, outs):
+        ref = alone(spec, fr, form)
+        assert len(got) == len(ref)
+        for n, (g, r) in enumerate(zip(got, ref)):
+            np.testing.assert_array_equal(g, r, err_msg=f"{spec['width']}x{spec['height']} frame {n}")
+
+
+def test_admission_by_budget_and_slots():
+    w, h = 640, 360
+    frame = synth.moving_rects(w, h, 1, 3, lo=16, hi=235, noise=2.0)[0]
+    with F.Server(form="fast", max_streams=2, hbm_budget=1 << 40) as sv:
+        a = sv.open(w, h, 8, 4, bt=3)
+        b = sv.open(w, h, 8, 4, bt=3)
+        assert a is not None and b is not None
+        assert sv.open(w, h, 8, 4, bt=3) is None  # no slot
+        sv.close_stream(a)
+        c = sv.open(w, h, 8, 4, bt=3)
+        assert c is not None
+        used = sv.stats()["used_bytes"]
+        sv.close_stream(b)
+        sv.close_stream(c)
+    # A budget that holds one such stream but not two.
+    with F.Server(form="fast", max_streams=8, hbm_budget=int(used * 0.75)) as sv:
+        a = sv.open(w, h, 8, 4, bt=3)
+        assert a is not None
+        assert sv.open(w, h, 8, 4, bt=3) is None  # over budget
+        for n in range(4):
+            assert sv.submit(a, n, frame)
+        got = [sv.poll(a, 5000) for _ in range(4)]
+        assert [g[0] for g in got] == [0, 1, 2, 3]
+        sv.close_stream(a)
+        assert sv.open(w, h, 8, 4, bt=3) is not None  # budget freed
