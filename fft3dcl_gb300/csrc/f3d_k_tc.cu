@@ -815,17 +815,24 @@ std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<d
       put_pair(t, T::B2HI, T::B2LO, tc::off_il(2 * ky + 1, 2 * y, 2 * N), -w * s);
       put_pair(t, T::B2HI, T::B2LO, tc::off_il(2 * ky + 1, 2 * y + 1, 2 * N), w * c);
     }
-  // Spectrum of the analysis window (the chroma offset's contribution).
+  // Spectrum of the analysis window (the chroma offset's contribution): the
+  // window is separable, so it is the product of the two axes' DFTs.
+  std::vector<double> ayr(N), ayi(N), axr(FBW), axi(FBW);
+  for (int k = 0; k < N; k++)
+    for (int j = 0; j < N; j++) {
+      double c, s;
+      cs(k, j, c, s);
+      ayr[k] += wy[j] * c;
+      ayi[k] -= wy[j] * s;
+      if (k < FBW) {
+        axr[k] += wx[j] * c;
+        axi[k] -= wx[j] * s;
+      }
+    }
   for (int ky = 0; ky < N; ky++)
     for (int kx = 0; kx < FBW; kx++) {
-      double re = 0.0, im = 0.0;
-      for (int y = 0; y < N; y++)
-        for (int x = 0; x < N; x++) {
-          const double th = 2.0 * kPiD * (double)((ky * y + kx * x) % N) / N;
-          re += wy[y] * wx[x] * std::cos(th);
-          im -= wy[y] * wx[x] * std::sin(th);
-        }
-      const float f[2] = {(float)re, (float)im};
+      const float f[2] = {(float)(ayr[ky] * axr[kx] - ayi[ky] * axi[kx]),
+                          (float)(ayr[ky] * axi[kx] + ayi[ky] * axr[kx])};
       std::memcpy(t.data() + T::WSPEC + (ky * FBW + kx) * 8, f, 8);
     }
   // C2 [2y+ro][2ky+ri]: complex column inverse DFT (unnormalised), synthesis

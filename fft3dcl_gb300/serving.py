@@ -3,8 +3,9 @@ frames arrive at their own rates, driven through a Server.
 
 ``mixed_streams`` draws the stream set (resolutions 640x360 .. 3840x2160,
 8- or 10-bit luma planes, bt in {1, 3, 4}, bw in {16, 32}, 24-60 frames/s),
-``run`` submits every stream's frames at Poisson arrival times, collects the
-outputs as they finish and returns them with the server's latency figures.
+``run`` opens the streams, submits every stream's frames at Poisson arrival
+times, collects the outputs as they finish and returns them with the
+server's latency figures.
 """
 from __future__ import annotations
 
@@ -45,12 +46,16 @@ def run(server: Server, specs: list[dict], frames: list[list[np.ndarray]], realt
     them when not realtime), polls outputs, closes finished streams. Returns
     each stream's outputs in frame order and the server statistics."""
     rng = np.random.default_rng(seed)
-    t0 = time.perf_counter()
     due = []
     for s in specs:
         gaps = rng.exponential(1.0 / s["fps"], s["frames"]) if realtime else np.zeros(s["frames"])
         due.append(np.cumsum(gaps))
     sid = [None] * len(specs)
+    # Clients connect first: every stream the server admits now is opened
+    # before the arrival clock starts; the others open as slots free up.
+    for i, s in enumerate(specs):
+        sid[i] = server.open(s["width"], s["height"], s["bits"], s["frames"], **s["params"])
+    t0 = time.perf_counter()
     nxt = [0] * len(specs)
     outs: list[list[np.ndarray]] = [[] for _ in specs]
     done = [False] * len(specs)
