@@ -100,6 +100,7 @@ EXPORTS = (
     "f3d_live_instances", "f3d_live_bytes", "f3d_kernel_launches", "f3d_denoise_noalloc",
     "f3d_server_create", "f3d_server_destroy", "f3d_server_open", "f3d_server_submit", "f3d_server_poll",
     "f3d_server_close", "f3d_server_get_stats",
+    "f3d_batch_create", "f3d_batch_destroy", "f3d_batch_error", "f3d_batch_step", "f3d_batch_tune",
 )
 
 _lib = None
@@ -138,6 +139,13 @@ def lib():
         L.f3d_process.argtypes = [vp, P(i), i, vp]
         L.f3d_process_raw.argtypes = [vp, P(i), i, vp, sz]
         L.f3d_process_device.argtypes = [vp, P(i), i, vp, sz]
+        L.f3d_batch_create.argtypes = [P(vp), i, i, P(vp)]
+        L.f3d_batch_destroy.argtypes = [vp]
+        L.f3d_batch_destroy.restype = None
+        L.f3d_batch_error.argtypes = [vp]
+        L.f3d_batch_error.restype = C.c_char_p
+        L.f3d_batch_step.argtypes = [vp, P(i), P(vp), P(sz), P(P(i)), P(i), P(vp), P(sz)]
+        L.f3d_batch_tune.argtypes = [vp, P(i), P(i)]
         L.f3d_server_create.argtypes = [P(ServerConfig), P(vp)]
         L.f3d_server_destroy.argtypes = [vp]
         L.f3d_server_destroy.restype = None
@@ -554,6 +562,60 @@ class Server:
     def close(self):
         if self._h:
             lib().f3d_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+BATCH_GRAPH = 1
+BATCH_AUTOTUNE = 2
+
+
+class Batch:
+    """One temporal step of up to four tensor-core engines (the planes of a
+    frame, or planes of several streams) with one launch per kernel
+    (f3d_batch_*); optionally replayed as a CUDA graph and autotuned."""
+
+    def __init__(self, engines: list, graph: bool = True, autotune: bool = True):
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(engines))(*[e._h.value for e in engines])
+        h = C.c_void_p()
+        flags = (BATCH_GRAPH if graph else 0) | (BATCH_AUTOTUNE if autotune else 0)
+        if lib().f3d_batch_create(arr, len(engines), flags, C.byref(h)) != F3D_OK:
+            raise F3DError(lib().f3d_last_error().decode())
+        self._h = h
+
+    def step(self, fns, srcs, src_pitches, windows, dsts, dst_pitches):
+        """fns[i]: frame entering plane i (-1: none) from device pointer
+        srcs[i]; windows[i]: the output window of plane i, written to device
+        pointer dsts[i]."""
+        n = len(self.engines)
+        wins = [(C.c_int * len(w))(*w) for w in windows]
+        wptr = (C.POINTER(C.c_int) * n)(*[C.cast(w, C.POINTER(C.c_int)) for w in wins])
+        rc = lib().f3d_batch_step(self._h, (C.c_int * n)(*fns), (C.c_void_p * n)(*srcs),
+                                  (C.c_size_t * n)(*src_pitches), wptr, (C.c_int * n)(*[len(w) for w in windows]),
+                                  (C.c_void_p * n)(*dsts), (C.c_size_t * n)(*dst_pitches))
+        if rc != F3D_OK:
+            raise F3DError(lib().f3d_batch_error(self._h).decode() or lib().f3d_last_error().decode())
+
+    def tune(self):
+        a, b = C.c_int(), C.c_int()
+        tuned = lib().f3d_batch_tune(self._h, C.byref(a), C.byref(b))
+        return {"tuned": bool(tuned), "fwd_ctas_per_sm": a.value, "filter_minb": b.value}
+
+    def close(self):
+        if self._h:
+            lib().f3d_batch_destroy(self._h)
             self._h = None
 
     def __enter__(self):

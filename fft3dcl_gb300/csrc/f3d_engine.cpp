@@ -59,6 +59,7 @@ struct f3d_engine {
   uint8_t* d_tc = nullptr;   // tensor-core form tables
   size_t tc_bytes = 0;
   int* d_err = nullptr;      // set by a tensor-core kernel whose wait gave up
+  TcTune tune;               // tensor-core launch shape
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int fbw = 0, ps = 0, bps = 1, fmt = FMT_U8;
@@ -182,6 +183,23 @@ void retire(f3d_engine* e, float2* m) {
     e->release(m, e->spec_bytes);
 }
 
+// Tensor-core forward arguments for frame fn whose spectra go to `spec`.
+TcFwdArgs tc_forward_args(const f3d_engine* e, const uint8_t* dsrc, long long pitch, int fmt, float2* spec) {
+  TcFwdArgs t{};
+  t.g = make_geo(e);
+  t.src = dsrc;
+  t.pitch = pitch;
+  t.fmt = fmt;
+  t.split = !(fmt == FMT_U8 || (fmt == FMT_U16 && e->geom.bits <= 11));
+  t.norm = e->norm;
+  t.out_scale = t.split ? 1.0f : (fmt == FMT_U8 ? 1.0f / 255.0f : e->norm);
+  t.chroma_norm = e->cnorm;
+  t.tab = e->d_tc;
+  t.spec = spec;
+  t.err = e->d_err;
+  return t;
+}
+
 int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int fmt) {
   float2* spec = spectra_slot(e, fn, true);
   if (!spec) return e->fail(F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
@@ -198,19 +216,8 @@ int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int
   cudaEventRecord(e->ev[0], e->stream);
   cudaError_t ce;
   if (e->form == F3D_FORM_TC) {
-    TcFwdArgs t{};
-    t.g = a.g;
-    t.src = dsrc;
-    t.pitch = pitch;
-    t.fmt = fmt;
-    t.split = !(fmt == FMT_U8 || (fmt == FMT_U16 && e->geom.bits <= 11));
-    t.norm = e->norm;
-    t.out_scale = t.split ? 1.0f : (fmt == FMT_U8 ? 1.0f / 255.0f : e->norm);
-    t.chroma_norm = e->cnorm;
-    t.tab = e->d_tc;
-    t.spec = spec;
-    t.err = e->d_err;
-    ce = launch_forward_tc(t, e->stream);
+    const TcFwdArgs t = tc_forward_args(e, dsrc, pitch, fmt, spec);
+    ce = launch_forward_tc_batch(&t, 1, e->tune, e->stream);
   } else {
     ce = launch_forward(e->form, a, e->stream);
   }
@@ -224,11 +231,12 @@ int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int
   return F3D_OK;
 }
 
-int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long long pitch, int fmt) {
+// Filter/inverse arguments of a window; fails on missing spectra.
+int inverse_args(f3d_engine* e, const int* window, int n, InvArgs& a) {
   const int need = e->ip.bm >= 2 ? e->ip.bt : 1;
   if (!window || n < need)
     return e->fail(F3D_E_PARAM, "FFT3DCL: the window must hold " + std::to_string(need) + " frame(s)");
-  InvArgs a{};
+  a = InvArgs{};
   for (int i = 0; i < 4; i++) {
     const int fn = window[i < need ? i : 0];
     const float2* s = spectra_slot(e, fn, false);
@@ -261,29 +269,43 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
   a.ssmax = e->ip.ssmax;
   a.kalman_cn = e->ip.kalman_cn;
   a.kr2 = e->ip.kratio * e->ip.kratio;
+  return F3D_OK;
+}
+
+// Sweep arguments (fused path) of a window's filter/inverse arguments.
+SweepArgs sweep_args(const f3d_engine* e, const InvArgs& a, uint8_t* ddst, long long pitch, int fmt) {
+  SweepArgs sa{};
+  sa.inv = a;
+  sa.dst = ddst;
+  sa.pitch = pitch;
+  sa.fmt = fmt;
+  sa.chroma_norm = e->cnorm;
+  sa.inv_norm = e->inv_norm;
+  sa.max_pix = e->max_pix;
+  sa.cells_x = (a.g.W + a.g.bw / 2 - 1) / (a.g.bw / 2);
+  sa.cells_y = (a.g.H + a.g.bh / 2 - 1) / (a.g.bh / 2);
+  sa.strips = e->sweep_strips;
+  sa.segs = e->sweep_segs;
+  sa.seam_w = sa.cells_x * (a.g.bw / 2);
+  sa.seam_b = e->d_seam;
+  sa.seam_t = e->d_seam ? e->d_seam + (size_t)(sa.segs - 1) * (a.g.bh / 2) * sa.seam_w : nullptr;
+  sa.prefetch = e->sweep_prefetch;
+  sa.tab = e->d_tc;
+  sa.err = e->d_err;
+  sa.img = e->d_img;
+  return sa;
+}
+
+int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long long pitch, int fmt) {
+  InvArgs a;
+  int rc = inverse_args(e, window, n, a);
+  if (rc != F3D_OK) return rc;
   if (e->fused) {
     // One fused launch (plus the seam merge) writes the packed plane.
-    SweepArgs sa{};
-    sa.inv = a;
-    sa.dst = ddst;
-    sa.pitch = pitch;
-    sa.fmt = fmt;
-    sa.chroma_norm = e->cnorm;
-    sa.inv_norm = e->inv_norm;
-    sa.max_pix = e->max_pix;
-    sa.cells_x = (a.g.W + a.g.bw / 2 - 1) / (a.g.bw / 2);
-    sa.cells_y = (a.g.H + a.g.bh / 2 - 1) / (a.g.bh / 2);
-    sa.strips = e->sweep_strips;
-    sa.segs = e->sweep_segs;
-    sa.seam_w = sa.cells_x * (a.g.bw / 2);
-    sa.seam_b = e->d_seam;
-    sa.seam_t = e->d_seam ? e->d_seam + (size_t)(sa.segs - 1) * (a.g.bh / 2) * sa.seam_w : nullptr;
-    sa.prefetch = e->sweep_prefetch;
-    sa.tab = e->d_tc;
-    sa.err = e->d_err;
-    sa.img = e->d_img;
+    const SweepArgs sa = sweep_args(e, a, ddst, pitch, fmt);
     cudaEventRecord(e->ev[2], e->stream);
-    cudaError_t ce = launch_sweep(e->inv_form, sa, e->stream, e->ev[4]);
+    cudaError_t ce = e->inv_form == F3D_FORM_TC ? launch_sweep_tc_batch(&sa, 1, e->tune, e->stream, e->ev[4])
+                                                : launch_sweep(e->inv_form, sa, e->stream, e->ev[4]);
     cudaEventRecord(e->ev[3], e->stream);
     e->proc_timed = true;
     if (ce != cudaSuccess) return e->cuda_fail(ce, "the fused filter/inverse/overlap-add launch");
@@ -720,3 +742,212 @@ size_t f3d_live_bytes(void) { return g_bytes.load(); }
 uint64_t f3d_kernel_launches(void) { return launch_count(); }
 
 }  // extern "C"
+
+// ---- batches of planes ------------------------------------------------------
+
+struct f3d_batch {
+  std::vector<f3d_engine*> eng;
+  int flags = 0;
+  cudaStream_t stream = nullptr;
+  TcTune tune;
+  bool tuned = false;
+  struct Graph {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    int kernels = 0;
+  };
+  std::map<unsigned, Graph> graphs;  // by the planes with a forward (bits 0-7) and an output (8-15)
+  std::string err;
+};
+
+namespace {
+
+// Autotuner results by batch shape, shared by all batches of the process.
+std::mutex g_tune_mtx;
+std::map<std::string, TcTune> g_tune_cache;
+
+std::string tune_key(const f3d_batch* b) {
+  std::string k;
+  for (const f3d_engine* e : b->eng)
+    k += std::to_string(e->geom.width) + "x" + std::to_string(e->geom.height) + "b" + std::to_string(e->fmt) + "m" +
+         std::to_string(e->ip.bm) + ";";
+  return k;
+}
+
+int batch_fail(f3d_batch* b, int code, const std::string& m) {
+  b->err = m;
+  return fail_thread(code, m);
+}
+
+}  // namespace
+
+extern "C" {
+
+int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** out) {
+  if (!engines || !out || n < 1 || n > kMaxBatch)
+    return fail_thread(F3D_E_PARAM, "FFT3DCL: a batch holds 1 to " + std::to_string(kMaxBatch) + " engines");
+  *out = nullptr;
+  const f3d_engine* e0 = engines[0];
+  for (int i = 0; i < n; i++) {
+    const f3d_engine* e = engines[i];
+    if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine in batch");
+    for (int j = 0; j < i; j++)
+      if (engines[j] == e) return fail_thread(F3D_E_PARAM, "FFT3DCL: an engine appears twice in the batch");
+    if (e->form != F3D_FORM_TC || e->inv_form != F3D_FORM_TC || !e->fused)
+      return fail_thread(F3D_E_UNSUPPORTED, "FFT3DCL: batches run the fused tensor-core form");
+    if (e->device != e0->device || e->stream != e0->stream)
+      return fail_thread(F3D_E_PARAM, "FFT3DCL: the engines of a batch share one device and stream");
+    if (e->ip.bw != e0->ip.bw || e->ip.bh != e0->ip.bh || e->ip.ow != e0->ip.ow || e->ip.oh != e0->ip.oh ||
+        e->ip.wintype != e0->ip.wintype || e->ip.bm != e0->ip.bm || e->fmt != e0->fmt)
+      return fail_thread(F3D_E_UNSUPPORTED,
+                         "FFT3DCL: the planes of a batch share block size, overlap, window, temporal mode and format");
+  }
+  auto* b = new f3d_batch();
+  b->eng.assign(engines, engines + n);
+  b->flags = flags;
+  b->stream = e0->stream;
+  std::lock_guard<std::mutex> lk(g_tune_mtx);
+  auto it = g_tune_cache.find(tune_key(b));
+  if (it != g_tune_cache.end()) {
+    b->tune = it->second;
+    b->tuned = true;
+  }
+  *out = b;
+  return F3D_OK;
+}
+
+void f3d_batch_destroy(f3d_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->eng[0]->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& kv : b->graphs) {
+    if (kv.second.x) cudaGraphExecDestroy(kv.second.x);
+    if (kv.second.g) cudaGraphDestroy(kv.second.g);
+  }
+  delete b;
+}
+
+const char* f3d_batch_error(f3d_batch* b) { return b ? b->err.c_str() : ""; }
+
+int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, const size_t* src_pitch,
+                   const int* const* windows, const int* nwin, void* const* dev_dst, const size_t* dst_pitch) {
+  if (!b || !fns || !dev_src || !src_pitch || !windows || !nwin || !dev_dst || !dst_pitch)
+    return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  const int n = (int)b->eng.size();
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (f3d_engine* e : b->eng) locks.emplace_back(e->mtx);
+  cudaSetDevice(b->eng[0]->device);
+  TcFwdArgs fa[kMaxBatch];
+  SweepArgs sa[kMaxBatch];
+  int nf = 0;
+  unsigned mask = 0;
+  for (int i = 0; i < n; i++) {
+    f3d_engine* e = b->eng[i];
+    if (fns[i] >= 0 && !e->cache.count(fns[i])) {
+      if (!dev_src[i] || src_pitch[i] < (size_t)e->geom.width * e->bps)
+        return batch_fail(b, F3D_E_PARAM, "FFT3DCL: bad source plane in batch");
+      float2* spec = spectra_slot(e, fns[i], true);
+      if (!spec) return batch_fail(b, F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
+      fa[nf++] = tc_forward_args(e, static_cast<const uint8_t*>(dev_src[i]), (long long)src_pitch[i], e->fmt, spec);
+      mask |= 1u << i;
+    }
+  }
+  int ns = 0;
+  for (int i = 0; i < n; i++) {
+    if (nwin[i] <= 0) continue;  // forward only
+    f3d_engine* e = b->eng[i];
+    InvArgs a;
+    int rc = inverse_args(e, windows[i], nwin[i], a);
+    if (rc != F3D_OK) return batch_fail(b, rc, e->err);
+    if (!dev_dst[i] || dst_pitch[i] < (size_t)e->geom.width * e->bps)
+      return batch_fail(b, F3D_E_PARAM, "FFT3DCL: bad output plane in batch");
+    sa[ns++] = sweep_args(e, a, static_cast<uint8_t*>(dev_dst[i]), (long long)dst_pitch[i], e->fmt);
+    mask |= 1u << (8 + i);
+  }
+  if (nf == 0 && ns == 0) return F3D_OK;
+  auto launch = [&](const TcTune& t) -> cudaError_t {
+    cudaError_t ce = nf ? launch_forward_tc_batch(fa, nf, t, b->stream) : cudaSuccess;
+    if (ce == cudaSuccess && ns) ce = launch_sweep_tc_batch(sa, ns, t, b->stream, nullptr);
+    return ce;
+  };
+  // Autotuner: on the first step in which every plane enters a new frame,
+  // time each candidate launch shape (the step's result is the same for
+  // all of them; the last run leaves it in place) and keep the fastest.
+  const unsigned all = (1u << n) - 1;
+  if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && mask == (all | (all << 8))) {
+    const TcTune cands[] = {{2, 5}, {1, 5}, {2, 4}, {1, 4}};
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; rep++)
+      for (const TcTune& c : cands) {
+        cudaEventRecord(t0, b->stream);
+        cudaError_t ce = launch(c);
+        cudaEventRecord(t1, b->stream);
+        if (ce == cudaSuccess) ce = cudaEventSynchronize(t1);
+        if (ce != cudaSuccess) {
+          cudaEventDestroy(t0);
+          cudaEventDestroy(t1);
+          return batch_fail(b, F3D_E_CUDA, std::string("FFT3DCL: autotune launch: ") + cudaGetErrorString(ce));
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        if (ms < best) {
+          best = ms;
+          b->tune = c;
+        }
+      }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    b->tuned = true;
+    std::lock_guard<std::mutex> lk(g_tune_mtx);
+    g_tune_cache[tune_key(b)] = b->tune;
+    return launch(b->tune) == cudaSuccess ? F3D_OK : batch_fail(b, F3D_E_CUDA, "FFT3DCL: batch launch failed");
+  }
+  cudaError_t ce = cudaSuccess;
+  if (b->flags & F3D_BATCH_GRAPH) {
+    // One CUDA graph per batch shape, captured at its first step; later steps
+    // re-point its kernel nodes at the step's buffers and replay it.
+    auto it = b->graphs.find(mask);
+    if (it == b->graphs.end()) {
+      f3d_batch::Graph gr;
+      ce = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed);
+      const long long l0 = f3d_kernel_launches();
+      if (ce == cudaSuccess) {
+        cudaError_t le = launch(b->tune);
+        ce = cudaStreamEndCapture(b->stream, &gr.g);
+        if (le != cudaSuccess) ce = le;
+      }
+      if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gr.x, gr.g, 0);
+      gr.kernels = (int)(f3d_kernel_launches() - l0);
+      if (ce == cudaSuccess) ce = cudaGraphLaunch(gr.x, b->stream);
+      if (ce != cudaSuccess) {
+        if (gr.x) cudaGraphExecDestroy(gr.x);
+        if (gr.g) cudaGraphDestroy(gr.g);
+        cudaGetLastError();
+        return batch_fail(b, F3D_E_CUDA, std::string("FFT3DCL: batch graph: ") + cudaGetErrorString(ce));
+      }
+      b->graphs[mask] = gr;
+      return F3D_OK;
+    }
+    ce = tc_graph_update(it->second.x, it->second.g, fa, nf, sa, ns);
+    if (ce == cudaSuccess) ce = cudaGraphLaunch(it->second.x, b->stream);
+    if (ce == cudaSuccess)
+      for (int k = 0; k < it->second.kernels; k++) count_launch();
+  } else {
+    ce = launch(b->tune);
+  }
+  if (ce != cudaSuccess) return batch_fail(b, F3D_E_CUDA, std::string("FFT3DCL: batch launch: ") + cudaGetErrorString(ce));
+  return F3D_OK;
+}
+
+int f3d_batch_tune(f3d_batch* b, int* fwd_ctas_per_sm, int* filter_minb) {
+  if (!b) return fail_thread(F3D_E_PARAM, "FFT3DCL: null batch");
+  if (fwd_ctas_per_sm) *fwd_ctas_per_sm = b->tune.fwd_ctas_per_sm;
+  if (filter_minb) *filter_minb = b->tune.filter_minb;
+  return b->tuned ? 1 : 0;
+}
+
+}  // extern "C"
+

@@ -191,8 +191,16 @@ __device__ __forceinline__ void deposit(const TcFwdArgs& a, uint8_t* a1, const u
   }
 }
 
+// Plane of a batch that item idx (a CTA, or a forward block group) belongs to.
+template <class Batch>
+__device__ __forceinline__ int plane_of(const Batch& b, const int (&prefix)[kMaxBatch + 1], int idx) {
+  int p = 0;
+  while (p + 1 < b.n && idx >= prefix[p + 1]) p++;
+  return p;
+}
+
 template <int N, int BPS>
-__global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_constant__ TcFwdArgs a) {
+__global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_constant__ TcFwdBatch B) {
   using C = TcCfg<N>;
   using L = FwdSmem<N>;
   using T = TcTab<N>;
@@ -204,12 +212,13 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
   float2* stage = reinterpret_cast<float2*>(sm + L::STAGE);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // Constant operands: B2 (hi, lo) and B1 (hi, lo) are contiguous in the table.
+  // Constant operands (the same for every plane of a batch): B2 (hi, lo) and
+  // B1 (hi, lo) are contiguous in the table.
   {
-    const uint4* src2 = reinterpret_cast<const uint4*>(a.tab + T::B2HI);
+    const uint4* src2 = reinterpret_cast<const uint4*>(B.p[0].tab + T::B2HI);
     uint4* dst2 = reinterpret_cast<uint4*>(sm + L::B2);
     for (int i = tid; i < (int)(2 * C::B2_BYTES / 16); i += kTcThreads) dst2[i] = src2[i];
-    const uint4* src1 = reinterpret_cast<const uint4*>(a.tab + T::B1HI);
+    const uint4* src1 = reinterpret_cast<const uint4*>(B.p[0].tab + T::B1HI);
     uint4* dst1 = reinterpret_cast<uint4*>(sm + L::B1);
     for (int i = tid; i < (int)(2 * C::B1_BYTES / 16); i += kTcThreads) dst1[i] = src1[i];
   }
@@ -226,13 +235,22 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const int ngroups = (a.g.nb + C::G - 1) / C::G;
+  const int ngroups = B.grp0[B.n];
   uint32_t phase = 0;
   uint4 raw[Gather<N, BPS>::TPT];
-  if ((int)blockIdx.x < ngroups) fetch<N, BPS>(a, blockIdx.x * C::G, min(C::G, a.g.nb - (int)blockIdx.x * C::G), raw);
+  // Raw samples of batch group g (the block group g - grp0[p] of plane p).
+  auto fetch_group = [&](int g) {
+    const int p = plane_of(B, B.grp0, g);
+    const TcFwdArgs& ap = B.p[p];
+    const int b = (g - B.grp0[p]) * C::G;
+    fetch<N, BPS>(ap, b, min(C::G, ap.g.nb - b), raw);
+  };
+  if ((int)blockIdx.x < ngroups) fetch_group(blockIdx.x);
 
   for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-    const int b0 = grp * C::G;
+    const int pl = plane_of(B, B.grp0, grp);
+    const TcFwdArgs& a = B.p[pl];
+    const int b0 = (grp - B.grp0[pl]) * C::G;
     const int nvalid = min(C::G, a.g.nb - b0);
     // The previous group's bulk store must have read the staging area, which
     // aliases the operands written next.
@@ -242,7 +260,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     // 1. This group's samples into A1; the next group's loads start.
     deposit<N, BPS>(a, sm + L::A1, raw);
     const int nxt = grp + gridDim.x;
-    if (nxt < ngroups) fetch<N, BPS>(a, nxt * C::G, min(C::G, a.g.nb - nxt * C::G), raw);
+    if (nxt < ngroups) fetch_group(nxt);
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -464,16 +482,19 @@ __device__ __forceinline__ void emit16(const SweepArgs& sa, int y, int x0, const
   }
 }
 
-template <int N, int BM>
-__global__ void __launch_bounds__(kTcThreads, F3D_TC_FILTER_MINB) k_filter_tc(const __grid_constant__ SweepArgs sa) {
+template <int N, int BM, int MINB>
+__global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_constant__ SweepBatch B) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
+  const int pl = plane_of(B, B.cta0, blockIdx.x);
+  const SweepArgs& sa = B.p[pl];
+  const int cta = blockIdx.x - B.cta0[pl];
   const InvArgs& a = sa.inv;
   extern __shared__ __align__(16) uint8_t smem_f[];
   float2* fbuf = reinterpret_cast<float2*>(smem_f);
   float* dcs = reinterpret_cast<float*>(smem_f + S::F_DC);
   const int tid = threadIdx.x;
-  const int strip = blockIdx.x % sa.strips, m = blockIdx.x / sa.strips;
+  const int strip = cta % sa.strips, m = cta / sa.strips;
   const int J0 = strip * S::TJ;
   const int ncols = a.g.ncols;
   const int nvbin = max(0, min(C::G, min(sa.cells_x + 1, ncols) - J0)) * C::PS;  // bins of needed blocks
@@ -541,7 +562,7 @@ __global__ void __launch_bounds__(kTcThreads, F3D_TC_FILTER_MINB) k_filter_tc(co
 }
 
 template <int N>
-__global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constant__ SweepArgs sa) {
+__global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constant__ SweepBatch B) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
   using T = TcTab<N>;
@@ -552,7 +573,10 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::TSLOT);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  const int strip = blockIdx.x % sa.strips, seg = blockIdx.x / sa.strips;
+  const int pl = plane_of(B, B.cta0, blockIdx.x);
+  const SweepArgs& sa = B.p[pl];
+  const int cta = blockIdx.x - B.cta0[pl];
+  const int strip = cta % sa.strips, seg = cta / sa.strips;
   const int J0 = strip * S::TJ;
   const int nrow = sa.cells_y + 1;
   const int M0 = (int)((long long)seg * nrow / sa.segs);
@@ -563,6 +587,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
   // Constant operands: C2 (hi, lo), then C1 A (hi, lo) and B (hi, lo).
   {
     const uint4* src2 = reinterpret_cast<const uint4*>(sa.tab + T::C2HI);
+    static_assert(sizeof(B) <= 32000, "kernel parameter space");
     uint4* dst2 = reinterpret_cast<uint4*>(sm + S::C2);
     for (int i = tid; i < (int)(2 * C::B2_BYTES / 16); i += kTcThreads) dst2[i] = src2[i];
     const uint4* src1 = reinterpret_cast<const uint4*>(sa.tab + T::C1AHI);
@@ -871,56 +896,187 @@ std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::
   return {};
 }
 
-cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st) {
-  if (a.g.bw != 32 || a.g.bh != 32 || a.g.mode != 1) return cudaErrorNotSupported;
+// The forward batch parameter of `planes` (false: not one batch).
+bool forward_batch(const TcFwdArgs* planes, int n, TcFwdBatch& B) {
   using C = TcCfg<32>;
+  if (n < 1 || n > kMaxBatch) return false;
+  B = TcFwdBatch{};
+  B.n = n;
+  for (int i = 0; i < n; i++) {
+    const TcFwdArgs& a = planes[i];
+    if (a.g.bw != 32 || a.g.bh != 32 || a.g.mode != 1 || a.fmt != planes[0].fmt) return false;
+    B.p[i] = a;
+    B.grp0[i + 1] = B.grp0[i] + (a.g.nb + C::G - 1) / C::G;
+  }
+  for (int i = n + 1; i <= kMaxBatch; i++) B.grp0[i] = B.grp0[n];
+  return true;
+}
+
+// The three sweep-side batch parameters (filter, inverse, seam merge) of
+// `planes`: the same planes, with the prefix of each kernel's CTA counts.
+bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& Bs, SweepBatch& Bm) {
+  if (n < 1 || n > kMaxBatch) return false;
+  SweepBatch B{};
+  B.n = n;
+  for (int i = 0; i < n; i++) {
+    const SweepArgs& a = planes[i];
+    if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm)
+      return false;
+    B.p[i] = a;
+  }
+  auto prefix = [&](SweepBatch& out, auto count) {
+    out = B;
+    for (int i = 0; i < n; i++) out.cta0[i + 1] = out.cta0[i] + count(out.p[i]);
+    for (int i = n + 1; i <= kMaxBatch; i++) out.cta0[i] = out.cta0[n];
+  };
+  prefix(Bf, [](const SweepArgs& a) { return a.strips * (a.cells_y + 1); });  // (row, strip) groups
+  prefix(Bs, [](const SweepArgs& a) { return a.strips * a.segs; });          // (strip, segment)
+  prefix(Bm, [](const SweepArgs& a) { return a.segs > 1 ? a.segs - 1 : 0; });  // seams
+  return true;
+}
+
+cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st) {
+  TcFwdBatch B;
+  if (!forward_batch(planes, n, B)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
   constexpr size_t smem = FwdSmem<32>::BYTES;
-  auto k = a.fmt == FMT_U8 ? k_forward_tc<32, 1> : a.fmt == FMT_U16 ? k_forward_tc<32, 2> : k_forward_tc<32, 4>;
+  const int fmt = planes[0].fmt;
+  auto k = fmt == FMT_U8 ? k_forward_tc<32, 1> : fmt == FMT_U16 ? k_forward_tc<32, 2> : k_forward_tc<32, 4>;
   cudaError_t attr = prepare(k, smem);
   if (attr != cudaSuccess) return attr;
-  const int ngroups = (a.g.nb + C::G - 1) / C::G;
+  const int ngroups = B.grp0[n];
   if (ngroups == 0) return cudaSuccess;
-  const int grid = std::min(ngroups, 2 * sm_count());
-  k<<<grid, kTcThreads, smem, st>>>(a);
+  const int grid = std::min(ngroups, std::max(1, std::min(t.fwd_ctas_per_sm, 2)) * sm_count());
+  k<<<grid, kTcThreads, smem, st>>>(B);
   count_launch();
   return cudaGetLastError();
 }
 
-template <int BM>
-cudaError_t launch_filter_bm(const SweepArgs& a, int nrow, cudaStream_t st) {
+cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st) { return launch_forward_tc_batch(&a, 1, TcTune{}, st); }
+
+template <int BM, int MINB>
+cudaError_t launch_filter_bm(const SweepBatch& B, cudaStream_t st) {
   constexpr size_t smem = SwpCfg<32>::F_BYTES;
-  auto k = k_filter_tc<32, BM>;
+  auto k = k_filter_tc<32, BM, MINB>;
   cudaError_t e = prepare(k, smem);
   if (e != cudaSuccess) return e;
-  k<<<a.strips * nrow, kTcThreads, smem, st>>>(a);
+  if (B.cta0[B.n] == 0) return cudaSuccess;
+  k<<<B.cta0[B.n], kTcThreads, smem, st>>>(B);
   count_launch();
   return cudaGetLastError();
 }
 
-cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
-  if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img) return cudaErrorNotSupported;
-  const int nrow = a.cells_y + 1;
-  cudaError_t e;
-  switch (a.inv.bm) {
-  case -1: e = launch_filter_bm<-1>(a, nrow, st); break;
-  case 1: e = launch_filter_bm<1>(a, nrow, st); break;
-  case 2: e = launch_filter_bm<2>(a, nrow, st); break;
-  case 3: e = launch_filter_bm<3>(a, nrow, st); break;
-  case 4: e = launch_filter_bm<4>(a, nrow, st); break;
+template <int MINB>
+cudaError_t launch_filter(const SweepBatch& B, int bm, cudaStream_t st) {
+  switch (bm) {
+  case -1: return launch_filter_bm<-1, MINB>(B, st);
+  case 1: return launch_filter_bm<1, MINB>(B, st);
+  case 2: return launch_filter_bm<2, MINB>(B, st);
+  case 3: return launch_filter_bm<3, MINB>(B, st);
+  case 4: return launch_filter_bm<4, MINB>(B, st);
   default: return cudaErrorNotSupported;
   }
+}
+
+// Finishes the seam cell rows of every plane of the batch: blockIdx.z runs
+// over all planes' seams (prefix in cta0), the sum as in k_seam_merge
+// (f3d_k_sweep.cu): ((q1 + q2) + q3) + q4, packed.
+__global__ void __launch_bounds__(256) k_seam_merge_batch(const __grid_constant__ SweepBatch B, int ch) {
+  const int pl = plane_of(B, B.cta0, blockIdx.z);
+  const SweepArgs& sa = B.p[pl];
+  const int k = blockIdx.z - B.cta0[pl];
+  const int x = blockIdx.x * 256 + threadIdx.x;
+  const int yy = blockIdx.y;
+  if (x >= sa.inv.g.W) return;
+  const int nrow = sa.cells_y + 1;
+  const int m1 = (int)((long long)(k + 1) * nrow / sa.segs);
+  const int y = (m1 - 1) * ch + yy;
+  if (y >= sa.inv.g.H) return;
+  const size_t o = ((size_t)k * ch + yy) * sa.seam_w + x;
+  const size_t ot = ((size_t)(k * 2) * ch + yy) * sa.seam_w + x;
+  float v = sa.seam_b[o] + sa.seam_t[ot];
+  v = v + sa.seam_t[ot + (size_t)ch * sa.seam_w];
+  if (sa.chroma_norm != 0.0f) v += sa.chroma_norm;
+  store_sample(sa.dst + (long long)y * sa.pitch, x, v, sa.fmt, sa.inv_norm, sa.max_pix);
+}
+
+cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
+                                  cudaEvent_t mark) {
+  SweepBatch Bf, B, Bm;
+  if (!sweep_batches(planes, n, Bf, B, Bm)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
+  const int bm = planes[0].inv.bm;
+  int maxw = 0;
+  for (int i = 0; i < n; i++) maxw = std::max(maxw, planes[i].inv.g.W);
+  // Filter: one CTA per (row, strip) group of every plane.
+  cudaError_t e = t.filter_minb == 4 ? launch_filter<4>(Bf, bm, st) : launch_filter<F3D_TC_FILTER_MINB>(Bf, bm, st);
   if (e != cudaSuccess) return e;
   if (mark) cudaEventRecord(mark, st);
+  // Inverse + overlap-add: one CTA per (strip, segment) of every plane.
   constexpr size_t smem = SwpCfg<32>::BYTES;
   static_assert(kTcSweepCtasPerSm * (SwpCfg<32>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
   static_assert(SwpCfg<32>::TJ == kTcSweepCells, "cells per strip");
   e = prepare(k_sweep_tc<32>, smem);
   if (e != cudaSuccess) return e;
-  k_sweep_tc<32><<<a.strips * a.segs, kTcThreads, smem, st>>>(a);
+  k_sweep_tc<32><<<B.cta0[n], kTcThreads, smem, st>>>(B);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return launch_seam_merge(a, st);
+  // Seam rows of all planes.
+  if (Bm.cta0[n] == 0) return cudaSuccess;
+  dim3 grid((maxw + 255) / 256, SwpCfg<32>::CH, Bm.cta0[n]);
+  k_seam_merge_batch<<<grid, 256, 0, st>>>(Bm, SwpCfg<32>::CH);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
+  return launch_sweep_tc_batch(&a, 1, TcTune{}, st, mark);
+}
+
+namespace {
+template <int MINB>
+bool is_filter(const void* f) {
+  return f == (const void*)k_filter_tc<32, -1, MINB> || f == (const void*)k_filter_tc<32, 1, MINB> ||
+         f == (const void*)k_filter_tc<32, 2, MINB> || f == (const void*)k_filter_tc<32, 3, MINB> ||
+         f == (const void*)k_filter_tc<32, 4, MINB>;
+}
+}  // namespace
+
+cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwdArgs* fwd, int nf,
+                            const SweepArgs* sw, int ns) {
+  TcFwdBatch Bw{};
+  SweepBatch Bf, Bs, Bm;
+  if (nf > 0 && !forward_batch(fwd, nf, Bw)) return cudaErrorNotSupported;
+  if (ns > 0 && !sweep_batches(sw, ns, Bf, Bs, Bm)) return cudaErrorNotSupported;
+  size_t cnt = 0;
+  cudaError_t e = cudaGraphGetNodes(graph, nullptr, &cnt);
+  if (e != cudaSuccess) return e;
+  std::vector<cudaGraphNode_t> nodes(cnt);
+  if ((e = cudaGraphGetNodes(graph, nodes.data(), &cnt)) != cudaSuccess) return e;
+  int ch = SwpCfg<32>::CH;
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType ty;
+    if ((e = cudaGraphNodeGetType(node, &ty)) != cudaSuccess) return e;
+    if (ty != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams kp{};
+    if ((e = cudaGraphKernelNodeGetParams(node, &kp)) != cudaSuccess) return e;
+    void* args[2] = {nullptr, &ch};
+    const void* f = kp.func;
+    if (f == (const void*)k_forward_tc<32, 1> || f == (const void*)k_forward_tc<32, 2> ||
+        f == (const void*)k_forward_tc<32, 4>)
+      args[0] = &Bw;
+    else if (is_filter<4>(f) || is_filter<F3D_TC_FILTER_MINB>(f))
+      args[0] = &Bf;
+    else if (f == (const void*)k_sweep_tc<32>)
+      args[0] = &Bs;
+    else if (f == (const void*)k_seam_merge_batch)
+      args[0] = &Bm;
+    else
+      return cudaErrorInvalidValue;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    if ((e = cudaGraphExecKernelNodeSetParams(exec, node, &kp)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 size_t tc_image_bytes(const Geo& g, int strips) {

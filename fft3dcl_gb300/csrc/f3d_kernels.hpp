@@ -152,6 +152,37 @@ std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::
                                const std::vector<double>& sxa, const std::vector<double>& sxb,
                                const std::vector<double>& sy);
 cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st);
+
+// Batches: up to kMaxBatch planes with the same block geometry, windows,
+// temporal mode and sample format in one launch of each kernel (the planes
+// of a YUV frame, or planes of several streams). A CTA finds its plane from
+// the prefix of per-plane CTA (forward: block-group) counts. Passed by value
+// as kernel parameters, so a captured CUDA graph is re-pointed at the next
+// frame's buffers by updating its kernel nodes' parameters.
+constexpr int kMaxBatch = 4;
+struct TcFwdBatch {
+  int n;
+  int grp0[kMaxBatch + 1];
+  TcFwdArgs p[kMaxBatch];
+};
+struct SweepBatch {
+  int n;
+  int cta0[kMaxBatch + 1];
+  SweepArgs p[kMaxBatch];
+};
+// Launch shape of the tensor-core kernels, picked by the autotuner.
+struct TcTune {
+  int fwd_ctas_per_sm = 2;  // persistent forward grid: CTAs per SM (1 or 2)
+  int filter_minb = 5;      // filter kernel variant: register budget for 5 or 4 CTAs per SM
+};
+cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st);
+cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
+                                  cudaEvent_t mark);
+// Re-points the kernel nodes of a graph captured from launch_forward_tc_batch
+// (nf planes, 0: none) + launch_sweep_tc_batch (ns planes) at new plane
+// arguments of the same shapes.
+cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwdArgs* fwd, int nf,
+                            const SweepArgs* sw, int ns);
 // Tensor-core sweep: cells per strip, CTAs per SM, and the launches (filter,
 // inverse + overlap-add, seam merge of f3d_k_sweep.cu).
 constexpr int kTcSweepCells = 7;

@@ -232,6 +232,35 @@ int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
                         const void* const* dev_window, int nwin, size_t src_pitch, void* dev_dst,
                         size_t dst_pitch, void* stream);
 
+/* ---- Batches of planes -----------------------------------------------------
+ * One temporal step of up to four planes (the planes of a YUV frame, or
+ * planes of several streams) with one launch per kernel: the forward
+ * transform of each plane's entering frame, then filter, inverse and
+ * overlap-add of each plane's window. The engines must run the fused
+ * tensor-core form (F3D_FORM_TC, half overlap, 32x32 blocks) on one device
+ * and one stream, with the same block size, overlap, window type, temporal
+ * mode and sample format; plane sizes and bit depths may differ.
+ * F3D_BATCH_GRAPH: each step shape is captured once as a CUDA graph and
+ * replayed with its kernel nodes re-pointed at the step's buffers.
+ * F3D_BATCH_AUTOTUNE: the first step in which every plane enters a frame
+ * times the candidate launch shapes (forward CTAs per SM, filter-kernel
+ * register budget) and keeps the fastest; results are cached per batch shape
+ * for the process. Results are the same as the engines' own calls. */
+#define F3D_BATCH_GRAPH 1
+#define F3D_BATCH_AUTOTUNE 2
+typedef struct f3d_batch f3d_batch;
+int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** out);
+void f3d_batch_destroy(f3d_batch* b);
+const char* f3d_batch_error(f3d_batch* b);
+/* Plane i: forward frame fns[i] from dev_src[i] (skipped when fns[i] < 0 or
+ * the frame is cached), then the output of window windows[i] (nwin[i]
+ * frames, as for f3d_process; nwin[i] = 0: no output) into dev_dst[i].
+ * Queued on the engines' stream. */
+int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, const size_t* src_pitch,
+                   const int* const* windows, const int* nwin, void* const* dev_dst, const size_t* dst_pitch);
+/* Launch shape in use; returns 1 when the autotuner has chosen it. */
+int f3d_batch_tune(f3d_batch* b, int* fwd_ctas_per_sm, int* filter_minb);
+
 /* ---- Serving loop ----------------------------------------------------------
  * Replaces the reference's one-instance-per-clip model (src/fft3dcl.cpp:289,
  * :365-368: VapourSynth requests serialised per instance by a mutex) for

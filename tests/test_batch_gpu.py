@@ -1,0 +1,103 @@
+"""Batches of tensor-core planes (f3d_batch_*): one launch per kernel for
+the planes of a YUV frame or of several streams, replayed as a CUDA graph and
+autotuned, give the same bits as each plane's own engine."""
+import numpy as np
+import pytest
+import torch
+
+import fft3dcl_gb300 as F
+from fft3dcl_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def run_planes(planes, params, chroma_flags, bits, batch_flags):
+    """planes[i]: list of frames of plane i. Returns outputs per plane, by
+    the batch when batch_flags is not None, else by separate engines."""
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.Stream(device=dev)
+    nfr = len(planes[0])
+    ip = F.validate(planes[0][0].shape[1], planes[0][0].shape[0], bits, **params)
+    bt, cur = ip.bt, ip.current
+    engines = [F.Engine(p[0].shape[1], p[0].shape[0], bits, chroma=c, form="tc", stream=st.cuda_stream, **params)
+               for p, c in zip(planes, chroma_flags)]
+    src = [torch.from_numpy(np.stack(p)).to(dev) for p in planes]
+    dst = [torch.empty(p[0].shape, dtype=src[i].dtype, device=dev) for i, p in enumerate(planes)]
+    outs = [[] for _ in planes]
+    pitch = [p[0].shape[1] * p[0].itemsize for p in planes]
+    b = F.Batch(engines, graph=bool(batch_flags & 1), autotune=bool(batch_flags & 2)) if batch_flags is not None else None
+    with torch.cuda.stream(st):
+        for n in range(nfr):
+            win = [min(max(n - cur + i, 0), nfr - 1) for i in range(bt)]
+            missing = sorted(set(win))
+            for fn in missing[:-1]:
+                for i, e in enumerate(engines):
+                    if not e.has(fn):
+                        if b is not None:
+                            b.step([fn if j == i else -1 for j in range(len(engines))],
+                                   [s[fn].data_ptr() for s in src], pitch, [[] for _ in engines],
+                                   [d.data_ptr() for d in dst], pitch)
+                        else:
+                            e.forward_device(fn, src[i][fn].data_ptr(), pitch[i])
+            last = missing[-1]
+            if b is not None:
+                b.step([last] * len(engines), [s[last].data_ptr() for s in src], pitch, [win] * len(engines),
+                       [d.data_ptr() for d in dst], pitch)
+            else:
+                for i, e in enumerate(engines):
+                    if not e.has(last):
+                        e.forward_device(last, src[i][last].data_ptr(), pitch[i])
+                    e.process_device(win, dst[i].data_ptr(), pitch[i])
+            st.synchronize()
+            for i, e in enumerate(engines):
+                outs[i].append(dst[i].cpu().numpy())
+                e.prune(n - cur - 1, n - cur + bt)
+    tune = b.tune() if b is not None else None
+    if b is not None:
+        b.close()
+    for e in engines:
+        e.close()
+    return outs, tune
+
+
+def yuv420(w, h, frames, seed, bits):
+    if bits == 8:
+        y = synth.moving_rects(w, h, frames, seed, lo=16, hi=235, noise=2.5)
+        u = synth.moving_rects(w // 2, h // 2, frames, seed + 1, lo=16, hi=240, noise=1.5, ramp=False)
+        v = synth.moving_rects(w // 2, h // 2, frames, seed + 2, lo=16, hi=240, noise=1.5, ramp=False)
+    else:
+        kw = dict(dtype=np.uint16, maxval=1023)
+        y = synth.moving_rects(w, h, frames, seed, lo=64, hi=940, noise=10.0, **kw)
+        u = synth.moving_rects(w // 2, h // 2, frames, seed + 1, lo=64, hi=960, noise=6.0, ramp=False, **kw)
+        v = synth.moving_rects(w // 2, h // 2, frames, seed + 2, lo=64, hi=960, noise=6.0, ramp=False, **kw)
+    return [y, u, v]
+
+
+@pytest.mark.parametrize("flags", [0, 1, 3])
+def test_yuv_planes_batch_equals_engines(flags):
+    planes = yuv420(480, 272, 7, 21, 8)
+    params = dict(sigma=2.5, bt=4, sharpen=0.4, scutoff=0.3, svr=1.0, smin=4.0, smax=20.0)
+    got, tune = run_planes(planes, params, [False, True, True], 8, flags)
+    ref, _ = run_planes(planes, params, [False, True, True], 8, None)
+    for i in range(3):
+        for n, (g, r) in enumerate(zip(got[i], ref[i])):
+            np.testing.assert_array_equal(g, r, err_msg=f"plane {i} frame {n}")
+    if flags & 2:
+        assert tune["tuned"] and tune["fwd_ctas_per_sm"] in (1, 2) and tune["filter_minb"] in (4, 5)
+
+
+def test_mixed_sizes_batch_equals_engines():
+    a = synth.moving_rects(640, 360, 6, 31, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
+    b = synth.moving_rects(1000, 200, 6, 32, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
+    params = dict(sigma=3.0, bt=3)
+    got, _ = run_planes([a, b], params, [False, False], 10, 3)
+    ref, _ = run_planes([a, b], params, [False, False], 10, None)
+    for i in range(2):
+        for g, r in zip(got[i], ref[i]):
+            np.testing.assert_array_equal(g, r)
+
+
+def test_batch_rejects_mixed_forms():
+    with F.Engine(96, 64, 8, form="tc", bt=3) as e1, F.Engine(96, 64, 8, form="fast", bt=3) as e2:
+        with pytest.raises(F.F3DError):
+            F.Batch([e1, e2])
