@@ -169,6 +169,77 @@ def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_
     return steps / dt, steps
 
 
+YUV_PARAMS = dict(sigma=2.5, bt=4, bw=32, bh=32, ow=16, oh=16, sharpen=0.4, scutoff=0.3, svr=1.0, smin=4.0,
+                  smax=20.0, degrid=1.0)
+
+
+def yuv_batched(args, dev, local_rank):
+    """1920x1080 YUV420P8, all three planes: the tensor-core form as one
+    batch (one launch per kernel for the three planes, replayed as a CUDA
+    graph, autotuned) against the fast form's per-plane engines."""
+    import torch
+    import fft3dcl_gb300 as F
+    from fft3dcl_gb300 import synth
+    w, h, nd = 1920, 1080, 8
+    planes = [synth.moving_rects(w, h, nd, 0xF3D0 + 1, lo=16, hi=235, noise=2.5),
+              synth.moving_rects(w // 2, h // 2, nd, 0xF3D0 + 11, lo=16, hi=240, noise=1.5, ramp=False),
+              synth.moving_rects(w // 2, h // 2, nd, 0xF3D0 + 12, lo=16, hi=240, noise=1.5, ramp=False)]
+    src = [torch.from_numpy(np.stack(p)).to(dev) for p in planes]
+    dst = [torch.empty(p[0].shape, dtype=torch.uint8, device=dev) for p in planes]
+    pitch = [p[0].shape[1] for p in planes]
+    ip = F.validate(w, h, 8, **YUV_PARAMS)
+    bt, cur = ip.bt, ip.current
+    res = {}
+    for form in ("tc", "fast"):
+        st = torch.cuda.Stream(device=dev)
+        engs = [F.Engine(p[0].shape[1], p[0].shape[0], 8, chroma=i > 0, form=form, device=local_rank,
+                         stream=st.cuda_stream, **YUV_PARAMS) for i, p in enumerate(planes)]
+        batch = F.Batch(engs, graph=True, autotune=True) if form == "tc" else None
+
+        def step(n):
+            win = [n - cur + i for i in range(bt)]
+            for fn in win[:-1]:
+                for i, e in enumerate(engs):
+                    if not e.has(fn):
+                        e.forward_device(fn, src[i][fn % nd].data_ptr(), pitch[i])
+            last = win[-1]
+            if batch is not None:
+                batch.step([last] * 3, [s[last % nd].data_ptr() for s in src], pitch, [win] * 3,
+                           [d.data_ptr() for d in dst], pitch)
+            else:
+                for i, e in enumerate(engs):
+                    if not e.has(last):
+                        e.forward_device(last, src[i][last % nd].data_ptr(), pitch[i])
+                    e.process_device(win, dst[i].data_ptr(), pitch[i])
+            for e in engs:
+                e.prune(n - cur - 1, n - cur + bt)
+
+        n = cur
+        for _ in range(max(3, args.warmup)):
+            step(n)
+            n += 1
+        torch.cuda.synchronize(dev)
+        l0 = F.kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            step(n)
+            n += 1
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1)
+        res[form] = {"frames_per_s": round(args.steps / (ms / 1000.0), 1),
+                     "launches_per_frame": round((F.kernel_launches() - l0) / args.steps, 2)}
+        if batch is not None:
+            res[form]["tune"] = batch.tune()
+            batch.close()
+        for e in engs:
+            e.close()
+    res["tc"]["form"] = "tensor cores, 3 planes per launch, CUDA graph per frame"
+    res["fast"]["form"] = "fp32 radix FFT, per-plane engines"
+    return res
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path on the host cores. The
     reference sources compile only here, so on the GPU host this is the C
@@ -352,6 +423,10 @@ def run_gpu(args, rank, world, local_rank):
                 "d2h_bytes_per_step": W * H * 2},
         "gpu_launches": int(launches), "clocks": clk,
     }
+    if world == 1 and not args.no_yuv:
+        line["yuv1080p_all_planes"] = dict(
+            workload="1920x1080 YUV420P8 all planes, sigma=2.5 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4 scutoff=0.3 "
+                     "svr=1 smin=4 smax=20 degrid=1, clip resident in HBM", **yuv_batched(args, dev, local_rank))
     if world == 1 and args.serve_streams > 0:
         # The serving workload: mixed streams with Poisson frame arrivals,
         # through the serving loop (continuous batching, HBM-budget admission).
@@ -394,6 +469,7 @@ def main():
                     help="comma-separated forms whose device throughput is reported under 'forms'")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-streams", type=int, default=16, help="streams of the serving run (0: skip it)")
+    ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
     ap.add_argument("--serve-frames", type=int, default=120, help="frames per serving stream")
     ap.add_argument("--frames", type=int, default=NFRAMES,
                     help="frames of the resident clip (fewer only to keep profiler captures small)")
