@@ -470,10 +470,16 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-streams", type=int, default=16, help="streams of the serving run (0: skip it)")
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
+    ap.add_argument("--size", default=None,
+                    help="WxH of the luma plane instead of 3840x2160 (small cases for profiling)")
     ap.add_argument("--serve-frames", type=int, default=120, help="frames per serving stream")
     ap.add_argument("--frames", type=int, default=NFRAMES,
                     help="frames of the resident clip (fewer only to keep profiler captures small)")
     args = ap.parse_args()
+    if args.size:
+        global W, H, WORKLOAD
+        W, H = (int(v) for v in args.size.lower().split("x"))
+        WORKLOAD = WORKLOAD.replace("3840x2160", f"{W}x{H}")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
