@@ -198,13 +198,15 @@ def yuv_batched(args, dev, local_rank):
 
         def step(n):
             win = [n - cur + i for i in range(bt)]
-            for fn in win[:-1]:
+            for fn in (win if batch is not None else win[:-1]):
                 for i, e in enumerate(engs):
                     if not e.has(fn):
                         e.forward_device(fn, src[i][fn % nd].data_ptr(), pitch[i])
             last = win[-1]
             if batch is not None:
-                batch.step([last] * 3, [s[last % nd].data_ptr() for s in src], pitch, [win] * 3,
+                # Forward one frame ahead, concurrent with this window's outputs.
+                ahead = n - cur + bt
+                batch.step([ahead] * 3, [s[ahead % nd].data_ptr() for s in src], pitch, [win] * 3,
                            [d.data_ptr() for d in dst], pitch)
             else:
                 for i, e in enumerate(engs):
@@ -235,7 +237,8 @@ def yuv_batched(args, dev, local_rank):
             batch.close()
         for e in engs:
             e.close()
-    res["tc"]["form"] = "tensor cores, 3 planes per launch, CUDA graph per frame"
+    res["tc"]["form"] = ("tensor cores, 3 planes per launch, CUDA graph per frame, forward one frame ahead "
+                         "concurrent with the outputs")
     res["fast"]["form"] = "fp32 radix FFT, per-plane engines"
     return res
 
@@ -283,19 +286,35 @@ def run_gpu(args, rank, world, local_rank):
         if world > 1:
             torch.distributed.barrier()
 
-    def device_run(form, with_clocks=False):
+    def device_run(form, with_clocks=False, batched=False):
         """Steady-state steps with the clip resident in HBM: (ms for
-        args.steps steps, per-kernel ms, launches, clocks, engine)."""
+        args.steps steps, per-kernel ms, launches, clocks, engine). Batched
+        (tensor-core form): each step is one batch step - forward of the frame
+        one ahead of the window, concurrent with the window's output - replayed
+        as a CUDA graph, launch shape autotuned; the per-kernel times come
+        from the engine's own calls."""
         stream = torch.cuda.Stream(device=dev)
         eng = F.Engine(W, H, BITS, form=form, device=local_rank, stream=stream.cuda_stream, **PARAMS)
+        batch = F.Batch([eng], graph=True, autotune=True) if batched else None
 
-        def step(n):
+        def step_engine(n):
             win = [n - cur + i for i in range(bt)]
             for fn in win:
                 if not eng.has(fn):
                     eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
             eng.process_device(win, out.data_ptr(), pitch)
             eng.prune(n - cur - 1, n - cur + bt)
+
+        def step_batch(n):
+            win = [n - cur + i for i in range(bt)]
+            for fn in win:
+                if not eng.has(fn):
+                    eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
+            ahead = n - cur + bt
+            batch.step([ahead], [clip_dev[ahead % nfr].data_ptr()], [pitch], [win], [out.data_ptr()], [pitch])
+            eng.prune(n - cur - 1, n - cur + bt)
+
+        step = step_batch if batched else step_engine
 
         n = cur
         for _ in range(max(3, args.warmup)):
@@ -323,24 +342,40 @@ def run_gpu(args, rank, world, local_rank):
         # after each step so that the engine's events can be read).
         kt = np.zeros(3)
         for _ in range(args.steps):
-            step(n)
+            step_engine(n)
             n += 1
             eng.synchronize()
             kt += np.array(eng.last_kernel_ms())
         kt /= args.steps
+        if batch is not None:
+            forms_extra["tune"] = batch.tune()
+            batch.close()
         return ms, kt, launches, clk, eng, stream, n
 
     # Other forms first (device throughput only), then the headline form.
     forms = {}
+    forms_extra = {}
     for f in [x for x in args.compare.split(",") if x and x != args.form]:
         ms_f, kt_f, _, _, eng_f, _, _ = device_run(f)
         forms[f] = {"value": round(args.steps * world / (ms_f / 1000.0), 3),
                     "kernel_ms": [round(float(x), 4) for x in kt_f]}
         eng_f.close()
-    ms, kt, launches, clk, eng, stream, n = device_run(args.form, with_clocks=True)
+    batched = args.form == "tc" and not args.no_batch
+    if batched:
+        # The tensor-core engine's own calls, for comparison with its batch.
+        ms_d, kt_d, _, _, eng_d, _, _ = device_run("tc")
+        forms["tc_direct"] = {"value": round(args.steps * world / (ms_d / 1000.0), 3),
+                              "kernel_ms": [round(float(x), 4) for x in kt_d],
+                              "how": "engine calls, forward then output, no graph"}
+        eng_d.close()
+    ms, kt, launches, clk, eng, stream, n = device_run(args.form, with_clocks=True, batched=batched)
     info = eng.info()
     forms[args.form] = {"value": round(args.steps * world / (ms / 1000.0), 3),
                         "kernel_ms": [round(float(x), 4) for x in kt]}
+    if batched:
+        forms[args.form]["how"] = ("batch step: forward one frame ahead concurrent with the window's output, "
+                                   "CUDA graph replay, autotuned launch shape")
+        forms[args.form]["tune"] = forms_extra.get("tune")
 
     # End to end through the C ABI with host buffers: pinned source planes,
     # upload of the entering frame and readback of the packed output.
@@ -470,6 +505,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-streams", type=int, default=16, help="streams of the serving run (0: skip it)")
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="tensor-core headline through the engine's own calls instead of a batch step")
     ap.add_argument("--size", default=None,
                     help="WxH of the luma plane instead of 3840x2160 (small cases for profiling)")
     ap.add_argument("--serve-frames", type=int, default=120, help="frames per serving stream")

@@ -756,8 +756,11 @@ struct f3d_batch {
     cudaGraphExec_t x = nullptr;
     int kernels = 0;
   };
-  std::map<unsigned, Graph> graphs;  // by the planes with a forward (bits 0-7) and an output (8-15)
+  std::map<unsigned, Graph> graphs;  // by the planes with a forward (bits 0-7), an output (8-15), overlap (16)
   std::string err;
+  // Side stream of the forward when it does not feed this step's outputs.
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -806,6 +809,14 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
   b->eng.assign(engines, engines + n);
   b->flags = flags;
   b->stream = e0->stream;
+  cudaSetDevice(e0->device);
+  if (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    f3d_batch_destroy(b);
+    return fail_thread(F3D_E_CUDA, "FFT3DCL: batch stream creation failed");
+  }
   std::lock_guard<std::mutex> lk(g_tune_mtx);
   auto it = g_tune_cache.find(tune_key(b));
   if (it != g_tune_cache.end()) {
@@ -820,10 +831,14 @@ void f3d_batch_destroy(f3d_batch* b) {
   if (!b) return;
   cudaSetDevice(b->eng[0]->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->side) cudaStreamSynchronize(b->side);
   for (auto& kv : b->graphs) {
     if (kv.second.x) cudaGraphExecDestroy(kv.second.x);
     if (kv.second.g) cudaGraphDestroy(kv.second.g);
   }
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->side) cudaStreamDestroy(b->side);
   delete b;
 }
 
@@ -865,8 +880,28 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
     mask |= 1u << (8 + i);
   }
   if (nf == 0 && ns == 0) return F3D_OK;
+  // When no plane's entering frame is in its own window (the caller runs one
+  // frame ahead), the forward does not feed this step's outputs: it runs on a
+  // side stream, concurrently with filter and inverse, and joins the main
+  // stream at the end of the step (the next step's outputs need it).
+  bool overlap = nf > 0 && ns > 0;
+  for (int i = 0; i < n && overlap; i++)
+    if (fns[i] >= 0 && (mask & (1u << i)))
+      for (int k = 0; k < nwin[i]; k++)
+        if (windows[i][k] == fns[i]) overlap = false;
+  if (overlap) mask |= 1u << 16;
   auto launch = [&](const TcTune& t) -> cudaError_t {
-    cudaError_t ce = nf ? launch_forward_tc_batch(fa, nf, t, b->stream) : cudaSuccess;
+    cudaError_t ce = cudaSuccess;
+    if (overlap) {
+      ce = cudaEventRecord(b->fork, b->stream);
+      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
+      if (ce == cudaSuccess) ce = launch_forward_tc_batch(fa, nf, t, b->side);
+      if (ce == cudaSuccess) ce = cudaEventRecord(b->join, b->side);
+      if (ce == cudaSuccess) ce = launch_sweep_tc_batch(sa, ns, t, b->stream, nullptr);
+      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->stream, b->join, 0);
+      return ce;
+    }
+    ce = nf ? launch_forward_tc_batch(fa, nf, t, b->stream) : cudaSuccess;
     if (ce == cudaSuccess && ns) ce = launch_sweep_tc_batch(sa, ns, t, b->stream, nullptr);
     return ce;
   };
@@ -874,7 +909,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   // time each candidate launch shape (the step's result is the same for
   // all of them; the last run leaves it in place) and keep the fastest.
   const unsigned all = (1u << n) - 1;
-  if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && mask == (all | (all << 8))) {
+  if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFu) == (all | (all << 8))) {
     const TcTune cands[] = {{2, 5}, {1, 5}, {2, 4}, {1, 4}};
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);

@@ -255,7 +255,10 @@ const char* f3d_batch_error(f3d_batch* b);
 /* Plane i: forward frame fns[i] from dev_src[i] (skipped when fns[i] < 0 or
  * the frame is cached), then the output of window windows[i] (nwin[i]
  * frames, as for f3d_process; nwin[i] = 0: no output) into dev_dst[i].
- * Queued on the engines' stream. */
+ * Queued on the engines' stream. When no entering frame is in its plane's
+ * window (the caller forwards one frame ahead: frame n+2 with output n at
+ * bt=4), the forward runs concurrently with the outputs on a second stream
+ * and joins the engines' stream before the step ends. */
 int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, const size_t* src_pitch,
                    const int* const* windows, const int* nwin, void* const* dev_dst, const size_t* dst_pitch);
 /* Launch shape in use; returns 1 when the autotuner has chosen it. */

@@ -11,7 +11,7 @@ from fft3dcl_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def run_planes(planes, params, chroma_flags, bits, batch_flags):
+def run_planes(planes, params, chroma_flags, bits, batch_flags, ahead=False):
     """planes[i]: list of frames of plane i. Returns outputs per plane, by
     the batch when batch_flags is not None, else by separate engines."""
     dev = torch.device("cuda", 0)
@@ -40,7 +40,16 @@ def run_planes(planes, params, chroma_flags, bits, batch_flags):
                         else:
                             e.forward_device(fn, src[i][fn].data_ptr(), pitch[i])
             last = missing[-1]
-            if b is not None:
+            if b is not None and ahead:
+                # Every window frame cached first; the step forwards the frame
+                # after the window, concurrently with the outputs.
+                for i, e in enumerate(engines):
+                    if not e.has(last):
+                        e.forward_device(last, src[i][last].data_ptr(), pitch[i])
+                nxt = min(win[-1] + 1, nfr - 1)
+                b.step([nxt] * len(engines), [s[nxt].data_ptr() for s in src], pitch, [win] * len(engines),
+                       [d.data_ptr() for d in dst], pitch)
+            elif b is not None:
                 b.step([last] * len(engines), [s[last].data_ptr() for s in src], pitch, [win] * len(engines),
                        [d.data_ptr() for d in dst], pitch)
             else:
@@ -84,6 +93,19 @@ def test_yuv_planes_batch_equals_engines(flags):
             np.testing.assert_array_equal(g, r, err_msg=f"plane {i} frame {n}")
     if flags & 2:
         assert tune["tuned"] and tune["fwd_ctas_per_sm"] in (1, 2) and tune["filter_minb"] in (4, 5)
+
+
+@pytest.mark.parametrize("flags", [0, 1])
+def test_lookahead_step_overlaps_and_equals_engines(flags):
+    # The forward of the frame after the window runs on the side stream,
+    # concurrently with the outputs (directly, or inside the captured graph).
+    planes = yuv420(320, 192, 8, 41, 10)
+    params = dict(sigma=3.0, bt=4, sharpen=0.3)
+    got, _ = run_planes(planes, params, [False, True, True], 10, flags, ahead=True)
+    ref, _ = run_planes(planes, params, [False, True, True], 10, None)
+    for i in range(3):
+        for n, (g, r) in enumerate(zip(got[i], ref[i])):
+            np.testing.assert_array_equal(g, r, err_msg=f"plane {i} frame {n}")
 
 
 def test_mixed_sizes_batch_equals_engines():
