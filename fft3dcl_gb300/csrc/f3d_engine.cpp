@@ -910,7 +910,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   // all of them; the last run leaves it in place) and keep the fastest.
   const unsigned all = (1u << n) - 1;
   if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFu) == (all | (all << 8))) {
-    const TcTune cands[] = {{2, 5}, {1, 5}, {2, 4}, {1, 4}};
+    const TcTune cands[] = {{2, 5}, {1, 5}, {2, 4}, {1, 4}, {2, 3}, {1, 3}};
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);

@@ -76,13 +76,9 @@ struct TcCfg {
 };
 
 constexpr int kTcThreads = 256;
-#ifndef F3D_TC_FILTER_BATCH
-#define F3D_TC_FILTER_BATCH 1
-#endif
-#ifndef F3D_TC_FILTER_MINB
-#define F3D_TC_FILTER_MINB 5  // filter-kernel CTAs per SM (register budget)
-#endif
-constexpr int kTcFilterBatch = F3D_TC_FILTER_BATCH;  // bins whose loads are in flight together
+// Filter-kernel variants: CTAs per SM and the bins whose loads are in flight
+// together; fewer CTAs leave registers for deeper batches.
+__host__ __device__ constexpr int filter_batch(int minb) { return minb >= 5 ? 1 : (minb == 4 ? 2 : 4); }
 constexpr uint64_t kWaitNs = 1000000000ull;  // one second
 
 // ---- forward ---------------------------------------------------------------
@@ -486,6 +482,7 @@ template <int N, int BM, int MINB>
 __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_constant__ SweepBatch B) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
+  constexpr int kTcFilterBatch = filter_batch(MINB);
   const int pl = plane_of(B, B.cta0, blockIdx.x);
   const SweepArgs& sa = B.p[pl];
   const int cta = blockIdx.x - B.cta0[pl];
@@ -509,6 +506,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   __syncthreads();
 
   // F. Bins tid + 256 j; the loads of kTcFilterBatch bins are issued together.
+  static_assert(kTcFilterBatch >= 1, "batch");
   const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
 #pragma unroll
   for (int j0 = 0; j0 < NB; j0 += kTcFilterBatch) {
@@ -1007,7 +1005,9 @@ cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& 
   int maxw = 0;
   for (int i = 0; i < n; i++) maxw = std::max(maxw, planes[i].inv.g.W);
   // Filter: one CTA per (row, strip) group of every plane.
-  cudaError_t e = t.filter_minb == 4 ? launch_filter<4>(Bf, bm, st) : launch_filter<F3D_TC_FILTER_MINB>(Bf, bm, st);
+  cudaError_t e = t.filter_minb == 3   ? launch_filter<3>(Bf, bm, st)
+                  : t.filter_minb == 4 ? launch_filter<4>(Bf, bm, st)
+                                       : launch_filter<5>(Bf, bm, st);
   if (e != cudaSuccess) return e;
   if (mark) cudaEventRecord(mark, st);
   // Inverse + overlap-add: one CTA per (strip, segment) of every plane.
@@ -1064,7 +1064,7 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
     if (f == (const void*)k_forward_tc<32, 1> || f == (const void*)k_forward_tc<32, 2> ||
         f == (const void*)k_forward_tc<32, 4>)
       args[0] = &Bw;
-    else if (is_filter<4>(f) || is_filter<F3D_TC_FILTER_MINB>(f))
+    else if (is_filter<3>(f) || is_filter<4>(f) || is_filter<5>(f))
       args[0] = &Bf;
     else if (f == (const void*)k_sweep_tc<32>)
       args[0] = &Bs;

@@ -173,7 +173,7 @@ struct SweepBatch {
 // Launch shape of the tensor-core kernels, picked by the autotuner.
 struct TcTune {
   int fwd_ctas_per_sm = 2;  // persistent forward grid: CTAs per SM (1 or 2)
-  int filter_minb = 5;      // filter kernel variant: register budget for 5 or 4 CTAs per SM
+  int filter_minb = 5;      // filter kernel variant: 5, 4 or 3 CTAs per SM (load batch 1, 2, 3 bins)
 };
 cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st);
 cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
