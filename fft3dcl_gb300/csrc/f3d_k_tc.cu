@@ -494,10 +494,16 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   const int strip = cta % sa.strips, m = cta / sa.strips;
   const int J0 = strip * S::TJ;
   const int ncols = a.g.ncols;
-  const int nvbin = max(0, min(C::G, min(sa.cells_x + 1, ncols) - J0)) * C::PS;  // bins of needed blocks
+  // A tile's eighth block is the next strip's first: that strip filters it
+  // and writes it into both tiles, so each block is filtered once. The last
+  // strip filters its own eighth block.
+  const bool last_strip = strip == sa.strips - 1;
+  const int own = last_strip ? C::G : C::G - 1;
+  const int nvbin = max(0, min(own, min(sa.cells_x + 1, ncols) - J0)) * C::PS;  // bins filtered here
   constexpr int NBIN = C::G * C::PS;
   constexpr int NB = NBIN / kTcThreads;
   static_assert(NBIN % kTcThreads == 0, "bins per thread");
+  constexpr int NF = BM >= 2 ? BM : 1;  // window frames read
 
   if (tid < C::G) {
     const int n = J0 + tid;
@@ -508,13 +514,21 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   // F. Bins tid + 256 j; the loads of kTcFilterBatch bins are issued together.
   static_assert(kTcFilterBatch >= 1, "batch");
   const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
+  // This thread's first bin in each window frame; bin j is kTcThreads * j
+  // further (constant offsets).
+  const float2* sp[NF];
+#pragma unroll
+  for (int k = 0; k < NF; k++) sp[k] = a.s[k] + gb0 + tid;
 #pragma unroll
   for (int j0 = 0; j0 < NB; j0 += kTcFilterBatch) {
     float2 sv[kTcFilterBatch][4];
 #pragma unroll
     for (int u = 0; u < kTcFilterBatch; u++) {
       const int i = tid + kTcThreads * (j0 + u);
-      if (j0 + u < NB && i < nvbin) load_window<BM>(a, gb0 + i, sv[u]);
+      if (j0 + u < NB && i < nvbin) {
+#pragma unroll
+        for (int k = 0; k < NF; k++) sv[u][k] = sp[k][kTcThreads * (j0 + u)];
+      }
     }
 #pragma unroll
     for (int u = 0; u < kTcFilterBatch; u++) {
@@ -529,10 +543,13 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   __syncthreads();
 
   // R. Row (k', block), K = 2 ky + (re, im) of the operand image, in 16-byte
-  // chunks of 4 ky.
+  // chunks of 4 ky. Block 0 also goes to the previous strip's tile as its
+  // block 7; this tile's block 7 comes from the next strip.
   uint8_t* img = sa.img + ((size_t)m * sa.strips + strip) * S::TILE;
+  uint8_t* prev = strip > 0 ? img - S::TILE : nullptr;
   const int r2 = tid & 127, h = tid >> 7;
   const int kp = r2 >> 3, bl = r2 & 7;
+  if (bl == C::G - 1 && !last_strip) return;
   const float2* fb = fbuf + bl * S::FS;
 #pragma unroll
   for (int cq = 0; cq < C::NY / 4; cq++) {
@@ -556,6 +573,11 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
     const uint32_t o = tc::off_sw128(r2, 2 * (C::NY * h + 4 * cq));
     *reinterpret_cast<uint4*>(img + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
     *reinterpret_cast<uint4*>(img + C::A2_BYTES + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    if (bl == 0 && prev) {
+      const uint32_t op = tc::off_sw128(r2 + C::G - 1, 2 * (C::NY * h + 4 * cq));
+      *reinterpret_cast<uint4*>(prev + op) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(prev + C::A2_BYTES + op) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
   }
 }
 
