@@ -76,6 +76,9 @@ struct TcCfg {
 };
 
 constexpr int kTcThreads = 256;
+#ifndef F3D_TC_FILTER_PREFETCH
+#define F3D_TC_FILTER_PREFETCH 1  // filter CTAs pull their group's spectra into L2 first
+#endif
 // Filter-kernel variants: CTAs per SM and the bins whose loads are in flight
 // together; fewer CTAs leave registers for deeper batches.
 __host__ __device__ constexpr int filter_batch(int minb) { return minb >= 5 ? 1 : (minb == 4 ? 2 : 4); }
@@ -505,6 +508,11 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   static_assert(NBIN % kTcThreads == 0, "bins per thread");
   constexpr int NF = BM >= 2 ? BM : 1;  // window frames read
 
+  const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
+  // The group's window spectra start moving into L2 as whole runs, so that
+  // the bins' loads below mostly wait on L2 rather than on DRAM.
+  if (F3D_TC_FILTER_PREFETCH && tid < NF && nvbin > 0)
+    tc::prefetch_l2(a.s[tid] + gb0, (uint32_t)(nvbin * sizeof(float2)));
   if (tid < C::G) {
     const int n = J0 + tid;
     dcs[tid] = (n <= sa.cells_x && n < ncols) ? block_dc(a, m * ncols + n) : 0.0f;
@@ -513,7 +521,6 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
 
   // F. Bins tid + 256 j; the loads of kTcFilterBatch bins are issued together.
   static_assert(kTcFilterBatch >= 1, "batch");
-  const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
   // This thread's first bin in each window frame; bin j is kTcThreads * j
   // further (constant offsets).
   const float2* sp[NF];
