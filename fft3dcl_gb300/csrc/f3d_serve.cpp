@@ -60,7 +60,7 @@ constexpr int kOutSlots = 3;  // outputs a stream may hold before they are polle
 struct InSlot {
   uint8_t* host = nullptr;  // pinned
   int frame = -1;
-  enum { FREE, FULL, UPLOADED } state = FREE;
+  enum { FREE, RESERVED, FULL, UPLOADED } state = FREE;  // RESERVED: a submit is copying into it
   long long seq = 0;        // output launch count when the upload was queued
   double t_arrive = 0.0;
 };
@@ -88,7 +88,6 @@ struct Stream {
   int next_out = 0;           // next output frame to launch
   long long seq = 0;
   std::vector<double> arrive; // arrival time of each input frame
-  bool closing = false;
   std::string err;
 };
 
@@ -200,7 +199,6 @@ void f3d_server::run() {
     for (auto& kv : streams) {
       Stream* s = kv.second;
       reap(s);
-      if (s->closing) continue;
       // Continuous batching: every stream whose next window is complete
       // gets its output launched in this pass.
       while (s->next_out < s->nframes && (int)s->outs.size() < kOutSlots && ready(s, s->next_out, win)) {
@@ -323,9 +321,8 @@ int f3d_server_submit(f3d_server* sv, int sid, int n, const void* src, long long
         break;
       }
     if (!slot) return fail(F3D_E_BUSY, "FFT3DCL: the stream's input slots are full");
-    slot->state = InSlot::UPLOADED;  // reserved while the copy below runs
+    slot->state = InSlot::RESERVED;  // held while the copy below runs
     slot->frame = -1;
-    slot->seq = -1;
   }
   const uint8_t* p = static_cast<const uint8_t*>(src);
   for (int y = 0; y < s->H; y++) std::memcpy(slot->host + y * s->row_bytes, p + y * pitch, s->row_bytes);
