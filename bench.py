@@ -286,16 +286,21 @@ def run_gpu(args, rank, world, local_rank):
         if world > 1:
             torch.distributed.barrier()
 
+    kout = args.outputs_per_step if (args.form == "tc" and not args.no_batch) else 1
+    outs = [out] + [torch.empty((H, W), dtype=torch.uint16, device=dev) for _ in range(kout - 1)]
+
     def device_run(form, with_clocks=False, batched=False):
         """Steady-state steps with the clip resident in HBM: (ms for
         args.steps steps, per-kernel ms, launches, clocks, engine). Batched
-        (tensor-core form): each step is one batch step - forward of the frame
-        one ahead of the window, concurrent with the window's output - replayed
-        as a CUDA graph, launch shape autotuned; the per-kernel times come
-        from the engine's own calls."""
+        (tensor-core form): each step is one batch step of kout consecutive
+        outputs - the forwards of the frames after their windows run
+        concurrently with the outputs - replayed as a CUDA graph, launch
+        shape autotuned; the per-kernel times come from the engine's own
+        calls. Returns the frames per step too."""
         stream = torch.cuda.Stream(device=dev)
         eng = F.Engine(W, H, BITS, form=form, device=local_rank, stream=stream.cuda_stream, **PARAMS)
-        batch = F.Batch([eng], graph=True, autotune=True) if batched else None
+        k = kout if batched else 1
+        batch = F.Batch([eng] * k, graph=True, autotune=True) if batched else None
 
         def step_engine(n):
             win = [n - cur + i for i in range(bt)]
@@ -306,20 +311,22 @@ def run_gpu(args, rank, world, local_rank):
             eng.prune(n - cur - 1, n - cur + bt)
 
         def step_batch(n):
-            win = [n - cur + i for i in range(bt)]
-            for fn in win:
-                if not eng.has(fn):
-                    eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
-            ahead = n - cur + bt
-            batch.step([ahead], [clip_dev[ahead % nfr].data_ptr()], [pitch], [win], [out.data_ptr()], [pitch])
-            eng.prune(n - cur - 1, n - cur + bt)
+            wins = [[m - cur + i for i in range(bt)] for m in range(n, n + k)]
+            for w in wins:
+                for fn in w:
+                    if not eng.has(fn):
+                        eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
+            ahead = [n + k - 1 - cur + bt + i for i in range(k)]  # the frames after the last window
+            batch.step(ahead, [clip_dev[a % nfr].data_ptr() for a in ahead], [pitch] * k, wins,
+                       [o.data_ptr() for o in outs[:k]], [pitch] * k)
+            eng.prune(n - cur - 1, n + k - 1 - cur + bt + k)
 
         step = step_batch if batched else step_engine
 
         n = cur
         for _ in range(max(3, args.warmup)):
             step(n)
-            n += 1
+            n += k
         torch.cuda.synchronize(dev)
         clocks = Clocks(local_rank) if with_clocks else None
         if clocks:
@@ -331,7 +338,7 @@ def run_gpu(args, rank, world, local_rank):
         e0.record(stream)
         for _ in range(args.steps):
             step(n)
-            n += 1
+            n += k
         e1.record(stream)
         torch.cuda.synchronize(dev)
         barrier()
@@ -350,31 +357,31 @@ def run_gpu(args, rank, world, local_rank):
         if batch is not None:
             forms_extra["tune"] = batch.tune()
             batch.close()
-        return ms, kt, launches, clk, eng, stream, n
+        return ms, kt, launches, clk, eng, stream, n, k
 
     # Other forms first (device throughput only), then the headline form.
     forms = {}
     forms_extra = {}
     for f in [x for x in args.compare.split(",") if x and x != args.form]:
-        ms_f, kt_f, _, _, eng_f, _, _ = device_run(f)
+        ms_f, kt_f, _, _, eng_f, _, _, _ = device_run(f)
         forms[f] = {"value": round(args.steps * world / (ms_f / 1000.0), 3),
                     "kernel_ms": [round(float(x), 4) for x in kt_f]}
         eng_f.close()
     batched = args.form == "tc" and not args.no_batch
     if batched:
         # The tensor-core engine's own calls, for comparison with its batch.
-        ms_d, kt_d, _, _, eng_d, _, _ = device_run("tc")
+        ms_d, kt_d, _, _, eng_d, _, _, _ = device_run("tc")
         forms["tc_direct"] = {"value": round(args.steps * world / (ms_d / 1000.0), 3),
                               "kernel_ms": [round(float(x), 4) for x in kt_d],
                               "how": "engine calls, forward then output, no graph"}
         eng_d.close()
-    ms, kt, launches, clk, eng, stream, n = device_run(args.form, with_clocks=True, batched=batched)
+    ms, kt, launches, clk, eng, stream, n, kframes = device_run(args.form, with_clocks=True, batched=batched)
     info = eng.info()
-    forms[args.form] = {"value": round(args.steps * world / (ms / 1000.0), 3),
+    forms[args.form] = {"value": round(args.steps * kframes * world / (ms / 1000.0), 3),
                         "kernel_ms": [round(float(x), 4) for x in kt]}
     if batched:
-        forms[args.form]["how"] = ("batch step: forward one frame ahead concurrent with the window's output, "
-                                   "CUDA graph replay, autotuned launch shape")
+        forms[args.form]["how"] = (f"batch step of {kout} consecutive outputs, the forwards of the frames after "
+                                   "their windows concurrent with them, CUDA graph replay, autotuned launch shape")
         forms[args.form]["tune"] = forms_extra.get("tune")
 
     # End to end with host buffers: pinned source planes, upload of the
@@ -389,38 +396,46 @@ def run_gpu(args, rank, world, local_rank):
     eng.prune(-1, -2)
     e2e_how = "engine forward_raw + process_raw per step (synchronous)"
     if batched:
+        k = kframes
         up = torch.cuda.Stream(device=dev)    # uploads
         down = torch.cuda.Stream(device=dev)  # readbacks
-        dsrc = [torch.empty((H, W), dtype=torch.uint16, device=dev) for _ in range(3)]
-        dout = [torch.empty((H, W), dtype=torch.uint16, device=dev) for _ in range(2)]
-        hout = [torch.empty((H, W), dtype=torch.uint16).pin_memory() for _ in range(2)]
+        dsrc = [[torch.empty((H, W), dtype=torch.uint16, device=dev) for _ in range(k)] for _ in range(3)]
+        dout = [[torch.empty((H, W), dtype=torch.uint16, device=dev) for _ in range(k)] for _ in range(2)]
+        hout = [[torch.empty((H, W), dtype=torch.uint16).pin_memory() for _ in range(k)] for _ in range(2)]
         ev_up = [torch.cuda.Event() for _ in range(3)]
         ev_comp = [torch.cuda.Event() for _ in range(3)]
         ev_read = [torch.cuda.Event() for _ in range(2)]
-        pbatch = F.Batch([eng], graph=True, autotune=True)
-        e2e_how = ("batch API pipeline: upload of frame n+2 and readback of output n on two copy streams, "
-                   "overlapping the batch step (forward n+2 concurrent with output n, CUDA graph)")
+        pbatch = F.Batch([eng] * k, graph=True, autotune=True)
+        e2e_how = (f"batch API pipeline, {k} outputs per step: uploads of the entering frames and readbacks of "
+                   "the outputs on two copy streams, overlapping the batch steps (forwards concurrent with the "
+                   "outputs, CUDA graph)")
+        step_no = [0]
 
         def step_host(n):
-            win = [n - cur + i for i in range(bt)]
-            for fn in win:
-                if not eng.has(fn):
-                    eng.forward_raw(fn, hnp[fn % len(hnp)])
-            ahead = n - cur + bt
-            k3, k2 = n % 3, n % 2
+            wins = [[m - cur + i for i in range(bt)] for m in range(n, n + k)]
+            for w in wins:
+                for fn in w:
+                    if not eng.has(fn):
+                        eng.forward_raw(fn, hnp[fn % len(hnp)])
+            ahead = [n + k - 1 - cur + bt + i for i in range(k)]
+            k3, k2 = step_no[0] % 3, step_no[0] % 2
+            step_no[0] += 1
             with torch.cuda.stream(up):
-                up.wait_event(ev_comp[k3])  # the forward that read this slot three steps ago
-                dsrc[k3].copy_(host[ahead % len(host)], non_blocking=True)
+                up.wait_event(ev_comp[k3])  # the forwards that read these slots three steps ago
+                for i, a in enumerate(ahead):
+                    dsrc[k3][i].copy_(host[a % len(host)], non_blocking=True)
                 ev_up[k3].record(up)
             stream.wait_event(ev_up[k3])
-            stream.wait_event(ev_read[k2])    # output slot read back two steps ago
-            pbatch.step([ahead], [dsrc[k3].data_ptr()], [pitch], [win], [dout[k2].data_ptr()], [pitch])
+            stream.wait_event(ev_read[k2])    # output slots read back two steps ago
+            pbatch.step(ahead, [d.data_ptr() for d in dsrc[k3]], [pitch] * k, wins,
+                        [d.data_ptr() for d in dout[k2]], [pitch] * k)
             ev_comp[k3].record(stream)
             with torch.cuda.stream(down):
                 down.wait_event(ev_comp[k3])
-                hout[k2].copy_(dout[k2], non_blocking=True)
+                for i in range(k):
+                    hout[k2][i].copy_(dout[k2][i], non_blocking=True)
                 ev_read[k2].record(down)
-            eng.prune(n - cur - 1, n - cur + bt)
+            eng.prune(n - cur - 1, n + k - 1 - cur + bt + k)
     else:
         hout = torch.empty((H, W), dtype=torch.uint16).pin_memory()
         hout_np = hout.numpy()
@@ -433,9 +448,10 @@ def run_gpu(args, rank, world, local_rank):
             eng.process_raw(win, hout_np)
             eng.prune(n - cur - 1, n - cur + bt)
 
+    kstep = kframes if batched else 1
     for _ in range(max(3, args.warmup)):
         step_host(n)
-        n += 1
+        n += kstep
     barrier()
     torch.cuda.synchronize(dev)
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -443,7 +459,7 @@ def run_gpu(args, rank, world, local_rank):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step_host(n)
-        n += 1
+        n += kstep
     if batched:
         stream.wait_stream(down)  # the last readbacks
     h1.record(stream)
@@ -461,8 +477,8 @@ def run_gpu(args, rank, world, local_rank):
         ms, ms_e2e = float(t[0]), float(t[1])
     if rank != 0:
         return
-    fps = args.steps * world / (ms / 1000.0)
-    fps_e2e = args.steps * world / (ms_e2e / 1000.0)
+    fps = args.steps * kframes * world / (ms / 1000.0)
+    fps_e2e = args.steps * kframes * world / (ms_e2e / 1000.0)
     ab = algorithmic_bytes(info.nblocks, info.fbw, ip.bh, bt)
     peak, peak_kind = load_peaks()
     inv_ms = float(kt[1])
@@ -485,7 +501,9 @@ def run_gpu(args, rank, world, local_rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded ramp + moving rectangles, Gaussian noise 12 LSB, 10-bit)",
-        "config": {"workload": WORKLOAD, "form": args.form, "parallelism": f"replicas x{world}",
+        "config": {"workload": WORKLOAD if kframes == 1 else WORKLOAD.replace(
+                       "one output frame per step", f"{kframes} consecutive output frames per step"),
+                   "form": args.form, "parallelism": f"replicas x{world}",
                    "inputs": f"clip resident in HBM ({len(frames)} x 16.6 MB)",
                    "l2": "working set per step ~750 MB: four 143 MB window spectra, larger than the 129 MB L2"},
         "kernel_ms": {kt_names[i]: round(float(kt[i]), 4) for i in range(3)},
@@ -498,8 +516,9 @@ def run_gpu(args, rank, world, local_rank):
         "roofline_step": {"algorithmic_bytes": ab["frame"],
                           "achieved": round(ab["frame"] * fps / world / 1e9, 1), "unit": "GB/s",
                           "frac": round(ab["frame"] * fps / world / 1e9 / peak, 4)},
-        "e2e": {"value": round(fps_e2e, 3), "unit": UNIT, "h2d_bytes_per_step": W * H * 2,
-                "d2h_bytes_per_step": W * H * 2, "how": e2e_how},
+        "e2e": {"value": round(fps_e2e, 3), "unit": UNIT, "h2d_bytes_per_step": W * H * 2 * kframes,
+                "d2h_bytes_per_step": W * H * 2 * kframes, "how": e2e_how},
+        "frames_per_step": kframes,
         "gpu_launches": int(launches), "clocks": clk,
     }
     if world == 1 and not args.no_yuv:
@@ -551,6 +570,8 @@ def main():
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
     ap.add_argument("--no-batch", action="store_true",
                     help="tensor-core headline through the engine's own calls instead of a batch step")
+    ap.add_argument("--outputs-per-step", type=int, default=2, choices=[1, 2, 3, 4],
+                    help="tensor-core batch: consecutive output frames per step")
     ap.add_argument("--size", default=None,
                     help="WxH of the luma plane instead of 3840x2160 (small cases for profiling)")
     ap.add_argument("--serve-frames", type=int, default=120, help="frames per serving stream")

@@ -14,6 +14,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -174,9 +175,10 @@ float2* spectra_slot(f3d_engine* e, int fn, bool create) {
 }
 
 // GpuRef::retireSpectra (src/cl/gpu.cpp:289-306): keep recycled buffers up
-// to 256 MiB, release the rest.
+// to 256 MiB, release the rest; at least two are kept, so that steps that
+// enter two frames (two outputs per batch step) do not allocate every time.
 void retire(f3d_engine* e, float2* m) {
-  const size_t budget = size_t(256) << 20;
+  const size_t budget = std::max(size_t(256) << 20, 2 * e->spec_bytes);
   if (e->pool.size() * e->spec_bytes + e->spec_bytes <= budget)
     e->pool.push_back(m);
   else
@@ -761,6 +763,11 @@ struct f3d_batch {
   // Side stream of the forward when it does not feed this step's outputs.
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  // Entries whose engine appeared earlier in the batch (one more output of
+  // that plane per step) have operand tiles and seam rows of their own.
+  std::vector<uint8_t*> img;   // per entry, null: the engine's own
+  std::vector<float*> seam;
+  std::vector<size_t> img_bytes, seam_bytes;
 };
 
 namespace {
@@ -794,8 +801,6 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
   for (int i = 0; i < n; i++) {
     const f3d_engine* e = engines[i];
     if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine in batch");
-    for (int j = 0; j < i; j++)
-      if (engines[j] == e) return fail_thread(F3D_E_PARAM, "FFT3DCL: an engine appears twice in the batch");
     if (e->form != F3D_FORM_TC || e->inv_form != F3D_FORM_TC || !e->fused)
       return fail_thread(F3D_E_UNSUPPORTED, "FFT3DCL: batches run the fused tensor-core form");
     if (e->device != e0->device || e->stream != e0->stream)
@@ -810,6 +815,24 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
   b->flags = flags;
   b->stream = e0->stream;
   cudaSetDevice(e0->device);
+  b->img.assign(n, nullptr);
+  b->seam.assign(n, nullptr);
+  b->img_bytes.assign(n, 0);
+  b->seam_bytes.assign(n, 0);
+  for (int i = 0; i < n; i++) {
+    bool repeat = false;
+    for (int j = 0; j < i; j++) repeat |= engines[j] == engines[i];
+    if (!repeat) continue;
+    const f3d_engine* e = engines[i];
+    b->img_bytes[i] = e->img_bytes;
+    b->seam_bytes[i] = sizeof(float) * e->seam_floats;
+    if (cudaMalloc(&b->img[i], b->img_bytes[i]) != cudaSuccess ||
+        (b->seam_bytes[i] && cudaMalloc(&b->seam[i], b->seam_bytes[i]) != cudaSuccess)) {
+      cudaGetLastError();
+      f3d_batch_destroy(b);
+      return fail_thread(F3D_E_NOMEM, "FFT3DCL: batch output buffers could not be allocated");
+    }
+  }
   if (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
@@ -839,6 +862,10 @@ void f3d_batch_destroy(f3d_batch* b) {
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
   if (b->side) cudaStreamDestroy(b->side);
+  for (uint8_t* p : b->img)
+    if (p) cudaFree(p);
+  for (float* p : b->seam)
+    if (p) cudaFree(p);
   delete b;
 }
 
@@ -850,7 +877,11 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
     return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
   const int n = (int)b->eng.size();
   std::vector<std::unique_lock<std::mutex>> locks;
-  for (f3d_engine* e : b->eng) locks.emplace_back(e->mtx);
+  for (int i = 0; i < n; i++) {
+    bool seen = false;
+    for (int j = 0; j < i; j++) seen |= b->eng[j] == b->eng[i];
+    if (!seen) locks.emplace_back(b->eng[i]->mtx);
+  }
   cudaSetDevice(b->eng[0]->device);
   TcFwdArgs fa[kMaxBatch];
   SweepArgs sa[kMaxBatch];
@@ -876,7 +907,13 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
     if (rc != F3D_OK) return batch_fail(b, rc, e->err);
     if (!dev_dst[i] || dst_pitch[i] < (size_t)e->geom.width * e->bps)
       return batch_fail(b, F3D_E_PARAM, "FFT3DCL: bad output plane in batch");
-    sa[ns++] = sweep_args(e, a, static_cast<uint8_t*>(dev_dst[i]), (long long)dst_pitch[i], e->fmt);
+    sa[ns] = sweep_args(e, a, static_cast<uint8_t*>(dev_dst[i]), (long long)dst_pitch[i], e->fmt);
+    if (b->img[i]) {  // a repeated engine: this output's own tiles and seam rows
+      sa[ns].img = b->img[i];
+      sa[ns].seam_b = b->seam[i];
+      sa[ns].seam_t = b->seam[i] ? b->seam[i] + (size_t)(sa[ns].segs - 1) * (a.g.bh / 2) * sa[ns].seam_w : nullptr;
+    }
+    ns++;
     mask |= 1u << (8 + i);
   }
   if (nf == 0 && ns == 0) return F3D_OK;
@@ -887,8 +924,10 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   bool overlap = nf > 0 && ns > 0;
   for (int i = 0; i < n && overlap; i++)
     if (fns[i] >= 0 && (mask & (1u << i)))
-      for (int k = 0; k < nwin[i]; k++)
-        if (windows[i][k] == fns[i]) overlap = false;
+      for (int j = 0; j < n; j++)
+        if (b->eng[j] == b->eng[i])
+          for (int k = 0; k < nwin[j]; k++)
+            if (windows[j][k] == fns[i]) overlap = false;
   if (overlap) mask |= 1u << 16;
   auto launch = [&](const TcTune& t) -> cudaError_t {
     cudaError_t ce = cudaSuccess;

@@ -486,9 +486,12 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
   constexpr int kTcFilterBatch = filter_batch(MINB);
-  const int pl = plane_of(B, B.cta0, blockIdx.x);
+  // Interleaved batches (outputs of one geometry, e.g. consecutive frames of
+  // a plane) run the same group of every output back to back, so that the
+  // window spectra they share are read from L2 the second time.
+  const int pl = B.interleave ? (int)(blockIdx.x % B.n) : plane_of(B, B.cta0, blockIdx.x);
   const SweepArgs& sa = B.p[pl];
-  const int cta = blockIdx.x - B.cta0[pl];
+  const int cta = B.interleave ? (int)(blockIdx.x / B.n) : (int)(blockIdx.x - B.cta0[pl]);
   const InvArgs& a = sa.inv;
   extern __shared__ __align__(16) uint8_t smem_f[];
   float2* fbuf = reinterpret_cast<float2*>(smem_f);
@@ -957,6 +960,10 @@ bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& B
     for (int i = n + 1; i <= kMaxBatch; i++) out.cta0[i] = out.cta0[n];
   };
   prefix(Bf, [](const SweepArgs& a) { return a.strips * (a.cells_y + 1); });  // (row, strip) groups
+  Bf.interleave = 1;
+  for (int i = 1; i < n; i++)
+    if (B.p[i].inv.g.W != B.p[0].inv.g.W || B.p[i].inv.g.H != B.p[0].inv.g.H || B.p[i].strips != B.p[0].strips)
+      Bf.interleave = 0;
   prefix(Bs, [](const SweepArgs& a) { return a.strips * a.segs; });          // (strip, segment)
   prefix(Bm, [](const SweepArgs& a) { return a.segs > 1 ? a.segs - 1 : 0; });  // seams
   return true;

@@ -168,6 +168,7 @@ struct TcFwdBatch {
 struct SweepBatch {
   int n;
   int cta0[kMaxBatch + 1];
+  int interleave;  // filter: planes of one geometry, CTA i is group i / n of plane i % n
   SweepArgs p[kMaxBatch];
 };
 // Launch shape of the tensor-core kernels, picked by the autotuner.

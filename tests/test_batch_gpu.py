@@ -92,7 +92,7 @@ def test_yuv_planes_batch_equals_engines(flags):
         for n, (g, r) in enumerate(zip(got[i], ref[i])):
             np.testing.assert_array_equal(g, r, err_msg=f"plane {i} frame {n}")
     if flags & 2:
-        assert tune["tuned"] and tune["fwd_ctas_per_sm"] in (1, 2) and tune["filter_minb"] in (4, 5)
+        assert tune["tuned"] and tune["fwd_ctas_per_sm"] in (1, 2) and tune["filter_minb"] in (3, 4, 5)
 
 
 @pytest.mark.parametrize("flags", [0, 1])
@@ -123,3 +123,37 @@ def test_batch_rejects_mixed_forms():
     with F.Engine(96, 64, 8, form="tc", bt=3) as e1, F.Engine(96, 64, 8, form="fast", bt=3) as e2:
         with pytest.raises(F.F3DError):
             F.Batch([e1, e2])
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_two_outputs_per_step_equal_engine(graph):
+    # The same engine twice in a batch: two consecutive outputs per step, the
+    # forwards of the next two frames concurrent with them.
+    frames = synth.moving_rects(320, 192, 11, 51, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
+    params = dict(sigma=3.0, bt=4, sharpen=0.3)
+    ref = F.FFT3DCL(frames, bits=10, form="tc", **params)
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.Stream(device=dev)
+    e = F.Engine(320, 192, 10, form="tc", stream=st.cuda_stream, **params)
+    src = torch.from_numpy(np.stack(frames)).to(dev)
+    dst = [torch.empty((192, 320), dtype=torch.uint16, device=dev) for _ in range(2)]
+    b = F.Batch([e, e], graph=graph, autotune=True)
+    nfr, pitch = len(frames), 320 * 2
+    got = []
+    with torch.cuda.stream(st):
+        for n in range(0, nfr, 2):
+            wins = [[min(max(m - 2 + i, 0), nfr - 1) for i in range(4)] for m in (n, n + 1)]
+            for w in wins:
+                for fn in w:
+                    if not e.has(fn):
+                        e.forward_device(fn, src[fn].data_ptr(), pitch)
+            ahead = [min(n + 3, nfr - 1), min(n + 4, nfr - 1)]
+            b.step(ahead, [src[a].data_ptr() for a in ahead], [pitch] * 2, wins,
+                   [d.data_ptr() for d in dst], [pitch] * 2)
+            st.synchronize()
+            got += [dst[0].cpu().numpy(), dst[1].cpu().numpy()]
+            e.prune(n - 3, n + 5)
+    b.close()
+    e.close()
+    for n in range(nfr):
+        np.testing.assert_array_equal(got[n], ref[n], err_msg=f"frame {n}")
