@@ -87,18 +87,24 @@ constexpr uint64_t kWaitNs = 1000000000ull;  // one second
 // ---- forward ---------------------------------------------------------------
 
 // Shared memory of the forward kernel (offsets from a 1024-aligned base).
-template <int N>
+// A1, A2 and the staging area of the spectra are live at the same time: the
+// next group's step-1 operand is deposited while step 2 of the current group
+// runs, and a group's bulk store drains while the next group is transformed.
+// Without the split (integer samples of up to 11 bits) A1 holds only the hi
+// parts, and two CTAs fit on an SM.
+template <int N, bool SPLIT>
 struct FwdSmem {
   using C = TcCfg<N>;
+  static constexpr uint32_t A1_TILE = (SPLIT ? 2 : 1) * C::A1_BYTES;  // hi[, lo] of one step-1 tile
   static constexpr uint32_t B2 = 0;                       // hi, lo
   static constexpr uint32_t B1 = B2 + 2 * C::B2_BYTES;    // hi, lo
   static constexpr uint32_t A2 = (B1 + 2 * C::B1_BYTES + 1023) / 1024 * 1024;  // hi, lo (SWIZZLE_128B)
   static constexpr uint32_t A1 = A2 + 2 * C::A2_BYTES;    // [tile][hi, lo]
-  static constexpr uint32_t STAGE = A2;                   // spectra of the group, after step 2
-  static constexpr uint32_t BAR = A1 + 2 * C::T1 * C::A1_BYTES;
+  static constexpr uint32_t STAGE = A1 + C::T1 * A1_TILE; // float2 [G][N][FBW]
+  static constexpr uint32_t BAR = STAGE + C::G * C::PS * 8;
   static constexpr uint32_t TSLOT = BAR + 16;
   static constexpr uint32_t BYTES = TSLOT + 16 + 1024;    // + alignment slack
-  static_assert(STAGE + C::G * C::PS * 8 <= BAR, "staging fits the operand space");
+  static_assert(STAGE % 16 == 0 && BAR % 16 == 0, "bulk-copy source alignment");
 };
 
 // Gather of a group's samples: task q covers 16 source bytes (16/BPS samples)
@@ -151,10 +157,11 @@ __device__ __forceinline__ void fetch(const TcFwdArgs& a, int b0, int nvalid, ui
 
 // Raw bytes -> fp16 (hi, and lo on the split path) in A1[tile][part]: rows
 // (block % BPT1, y), K = x.
-template <int N, int BPS>
+template <int N, int BPS, bool SPLIT>
 __device__ __forceinline__ void deposit(const TcFwdArgs& a, uint8_t* a1, const uint4 (&r)[Gather<N, BPS>::TPT]) {
   using Gt = Gather<N, BPS>;
   using C = TcCfg<N>;
+  const bool split = SPLIT && a.split;
 #pragma unroll
   for (int i = 0; i < Gt::TPT; i++) {
     const int q = threadIdx.x + i * kTcThreads;
@@ -166,26 +173,26 @@ __device__ __forceinline__ void deposit(const TcFwdArgs& a, uint8_t* a1, const u
 #pragma unroll
     for (int k = 0; k < Gt::S; k++) {
       if (BPS == 1) v[k] = (float)((w[k >> 2] >> (8 * (k & 3))) & 0xffu);
-      else if (BPS == 2) v[k] = (float)((w[k >> 1] >> (16 * (k & 1))) & 0xffffu) * (a.split ? a.norm : 1.0f);
+      else if (BPS == 2) v[k] = (float)((w[k >> 1] >> (16 * (k & 1))) & 0xffffu) * (split ? a.norm : 1.0f);
       else v[k] = __uint_as_float(w[k]);
     }
     uint32_t h[Gt::S / 2], l[Gt::S / 2];
 #pragma unroll
     for (int k = 0; k < Gt::S / 2; k++) tc::split_pair(v[2 * k], v[2 * k + 1], h[k], l[k]);
-    uint8_t* t0 = a1 + tile * 2 * C::A1_BYTES;
+    uint8_t* t0 = a1 + tile * FwdSmem<N, SPLIT>::A1_TILE;
     const int x0 = c * Gt::S;
     if (Gt::S >= 8) {
 #pragma unroll
       for (int j = 0; j < Gt::S / 8; j++) {
         const uint32_t o = tc::off_il(row, x0 + 8 * j, C::K1);
         *reinterpret_cast<uint4*>(t0 + o) = make_uint4(h[4 * j], h[4 * j + 1], h[4 * j + 2], h[4 * j + 3]);
-        if (a.split)
+        if (split)
           *reinterpret_cast<uint4*>(t0 + C::A1_BYTES + o) = make_uint4(l[4 * j], l[4 * j + 1], l[4 * j + 2], l[4 * j + 3]);
       }
     } else {
       const uint32_t o = tc::off_il(row, x0, C::K1);
       *reinterpret_cast<uint2*>(t0 + o) = make_uint2(h[0], h[1]);
-      if (a.split) *reinterpret_cast<uint2*>(t0 + C::A1_BYTES + o) = make_uint2(l[0], l[1]);
+      if (split) *reinterpret_cast<uint2*>(t0 + C::A1_BYTES + o) = make_uint2(l[0], l[1]);
     }
   }
 }
@@ -198,10 +205,10 @@ __device__ __forceinline__ int plane_of(const Batch& b, const int (&prefix)[kMax
   return p;
 }
 
-template <int N, int BPS>
+template <int N, int BPS, bool SPLIT>
 __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_constant__ TcFwdBatch B) {
   using C = TcCfg<N>;
-  using L = FwdSmem<N>;
+  using L = FwdSmem<N, SPLIT>;
   using T = TcTab<N>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -244,33 +251,23 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     const int b = (g - B.grp0[p]) * C::G;
     fetch<N, BPS>(ap, b, min(C::G, ap.g.nb - b), raw);
   };
-  if ((int)blockIdx.x < ngroups) fetch_group(blockIdx.x);
-
-  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-    const int pl = plane_of(B, B.grp0, grp);
-    const TcFwdArgs& a = B.p[pl];
-    const int b0 = (grp - B.grp0[pl]) * C::G;
-    const int nvalid = min(C::G, a.g.nb - b0);
-    // The previous group's bulk store must have read the staging area, which
-    // aliases the operands written next.
-    if (tid == 0) tc::bulk_wait_read();
-    __syncthreads();
-
-    // 1. This group's samples into A1; the next group's loads start.
-    deposit<N, BPS>(a, sm + L::A1, raw);
-    const int nxt = grp + gridDim.x;
-    if (nxt < ngroups) fetch_group(nxt);
+  // Group g (its samples in raw) into A1, the loads of the CTA's group after
+  // it started, then step 1 on the tensor cores: D1[tile] = A1 * B1^T, two or
+  // three passes, committed to bar[0]. A1 and D1 must be free: no step 1 in
+  // flight, D1 read out.
+  auto begin_group = [&](int g) {
+    const TcFwdArgs& ap = B.p[plane_of(B, B.grp0, g)];
+    deposit<N, BPS, SPLIT>(ap, sm + L::A1, raw);
+    if (g + (int)gridDim.x < ngroups) fetch_group(g + gridDim.x);
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
-
-    // 2. Step 1 on the tensor cores: D1[tile] = A1 * B1^T (two or three passes).
     if (tid == 0) {
       tc::fence_after_sync();
       constexpr uint32_t id1 = tc::idesc_f16(128, C::N1);
       const uint32_t sbo = (C::K1 / 8) * 128;
       for (int t = 0; t < C::T1; t++) {
-        const uint32_t a_hi = sbase + L::A1 + t * 2 * C::A1_BYTES, a_lo = a_hi + C::A1_BYTES;
+        const uint32_t a_hi = sbase + L::A1 + t * L::A1_TILE, a_lo = a_hi + C::A1_BYTES;
         const uint32_t d = tmem + C::D1_COL + t * C::N1;
         for (int ks = 0; ks < C::K1 / 16; ks++) {
           const uint64_t ah = tc::sdesc(a_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
@@ -278,11 +275,27 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
           const uint64_t bl = tc::sdesc(sbase + L::B1 + C::B1_BYTES + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
           tc::mma_f16(d, ah, bh, id1, ks > 0);
           tc::mma_f16(d, ah, bl, id1, 1);
-          if (a.split) tc::mma_f16(d, tc::sdesc(a_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE), bh, id1, 1);
+          if (SPLIT && ap.split)
+            tc::mma_f16(d, tc::sdesc(a_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE), bh, id1, 1);
         }
       }
       tc::mma_commit(&bar[0]);
     }
+  };
+  if ((int)blockIdx.x < ngroups) {
+    fetch_group(blockIdx.x);
+    begin_group(blockIdx.x);
+  }
+
+  // Per group: step 1 was issued one iteration earlier; step 2 runs while
+  // the next group's samples are deposited and its step 1 issued; the
+  // spectra are staged and leave by one bulk copy, which drains while the
+  // next group goes through steps 1 to 5.
+  for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const int pl = plane_of(B, B.grp0, grp);
+    const TcFwdArgs& a = B.p[pl];
+    const int b0 = (grp - B.grp0[pl]) * C::G;
+    const int nvalid = min(C::G, a.g.nb - b0);
     // Every thread takes the same branch: a wait that gave up anywhere ends
     // the sweep of groups for the whole CTA.
     if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
@@ -328,6 +341,12 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
       }
       tc::mma_commit(&bar[1]);
     }
+
+    // 5. The next group's operand and step 1 (every warp has read D1 above).
+    if (grp + (int)gridDim.x < ngroups) begin_group(grp + gridDim.x);
+
+    // The previous group's bulk store must have read the staging area.
+    if (tid == 0) tc::bulk_wait_read();
     if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
       if (tid == 0) atomicOr(a.err, 1);
       break;
@@ -335,7 +354,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     phase ^= 1;
     tc::fence_after_sync();
 
-    // 5. D2 -> staging [block][ky][kx], scaled; column 0 holds the packed P.
+    // 6. D2 -> staging [block][ky][kx], scaled; column 0 holds the packed P.
     {
       const int s = warp & 3, h = warp >> 2;
       const int r2 = 32 * s + lane;
@@ -349,12 +368,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
         o[ky * C::FBW] = make_float2(v[2 * j] * a.out_scale, v[2 * j + 1] * a.out_scale);
       }
     }
-    tc::fence_before_sync();
     __syncthreads();
 
-    // 6. Unpack columns 0 and n/2; chroma offset.
-    for (int q = tid; q < C::G * N; q += kTcThreads) {
-      const int bl = q / N, ky = q % N;
+    // 7. Unpack columns 0 and n/2; chroma offset.
+    {
+      const int bl = tid / N, ky = tid % N;
       float2* blk = stage + bl * C::PS;
       const float2 P = blk[ky * C::FBW], Q = blk[((N - ky) % N) * C::FBW];
       __syncwarp();
@@ -374,7 +392,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     tc::fence_async_smem();
     __syncthreads();
 
-    // 7. One bulk copy of the group's spectra to HBM.
+    // 8. One bulk copy of the group's spectra to HBM.
     if (tid == 0 && nvalid > 0) {
       tc::bulk_store(a.spec + (size_t)b0 * C::PS, stage, (uint32_t)(nvalid * C::PS * 8));
       tc::bulk_commit();
@@ -972,14 +990,22 @@ bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& B
 cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st) {
   TcFwdBatch B;
   if (!forward_batch(planes, n, B)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
-  constexpr size_t smem = FwdSmem<32>::BYTES;
+  // The split kernel (hi + lo step-1 operand) also takes planes that need no
+  // split; it fits one CTA per SM, the other two.
+  bool split = false;
+  for (int i = 0; i < n; i++) split = split || planes[i].split;
   const int fmt = planes[0].fmt;
-  auto k = fmt == FMT_U8 ? k_forward_tc<32, 1> : fmt == FMT_U16 ? k_forward_tc<32, 2> : k_forward_tc<32, 4>;
+  if (fmt == FMT_U8 && split) return cudaErrorNotSupported;
+  auto k = fmt == FMT_U8 ? k_forward_tc<32, 1, false>
+           : fmt == FMT_U16 ? (split ? k_forward_tc<32, 2, true> : k_forward_tc<32, 2, false>)
+                            : k_forward_tc<32, 4, true>;
+  const size_t smem = split ? FwdSmem<32, true>::BYTES : FwdSmem<32, false>::BYTES;
   cudaError_t attr = prepare(k, smem);
   if (attr != cudaSuccess) return attr;
   const int ngroups = B.grp0[n];
   if (ngroups == 0) return cudaSuccess;
-  const int grid = std::min(ngroups, std::max(1, std::min(t.fwd_ctas_per_sm, 2)) * sm_count());
+  const int per_sm = split ? 1 : std::max(1, std::min(t.fwd_ctas_per_sm, 2));
+  const int grid = std::min(ngroups, per_sm * sm_count());
   k<<<grid, kTcThreads, smem, st>>>(B);
   count_launch();
   return cudaGetLastError();
@@ -1097,8 +1123,8 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
     if ((e = cudaGraphKernelNodeGetParams(node, &kp)) != cudaSuccess) return e;
     void* args[2] = {nullptr, &ch};
     const void* f = kp.func;
-    if (f == (const void*)k_forward_tc<32, 1> || f == (const void*)k_forward_tc<32, 2> ||
-        f == (const void*)k_forward_tc<32, 4>)
+    if (f == (const void*)k_forward_tc<32, 1, false> || f == (const void*)k_forward_tc<32, 2, false> ||
+        f == (const void*)k_forward_tc<32, 2, true> || f == (const void*)k_forward_tc<32, 4, true>)
       args[0] = &Bw;
     else if (is_filter<3>(f) || is_filter<4>(f) || is_filter<5>(f))
       args[0] = &Bf;
