@@ -101,6 +101,7 @@ EXPORTS = (
     "f3d_server_create", "f3d_server_destroy", "f3d_server_open", "f3d_server_submit", "f3d_server_poll",
     "f3d_server_close", "f3d_server_get_stats",
     "f3d_batch_create", "f3d_batch_destroy", "f3d_batch_error", "f3d_batch_step", "f3d_batch_tune",
+    "f3d_batch_set_tune",
 )
 
 _lib = None
@@ -146,6 +147,7 @@ def lib():
         L.f3d_batch_error.restype = C.c_char_p
         L.f3d_batch_step.argtypes = [vp, P(i), P(vp), P(sz), P(P(i)), P(i), P(vp), P(sz)]
         L.f3d_batch_tune.argtypes = [vp, P(i), P(i)]
+        L.f3d_batch_set_tune.argtypes = [vp, i, i]
         L.f3d_server_create.argtypes = [P(ServerConfig), P(vp)]
         L.f3d_server_destroy.argtypes = [vp]
         L.f3d_server_destroy.restype = None
@@ -612,6 +614,11 @@ class Batch:
         a, b = C.c_int(), C.c_int()
         tuned = lib().f3d_batch_tune(self._h, C.byref(a), C.byref(b))
         return {"tuned": bool(tuned), "fwd_ctas_per_sm": a.value, "filter_minb": b.value}
+
+    def set_tune(self, fwd_ctas_per_sm: int, filter_minb: int):
+        """Pins the launch shape (every shape gives the same results)."""
+        if lib().f3d_batch_set_tune(self._h, fwd_ctas_per_sm, filter_minb) != F3D_OK:
+            raise F3DError(lib().f3d_batch_error(self._h).decode())
 
     def close(self):
         if self._h:

@@ -1023,5 +1023,22 @@ int f3d_batch_tune(f3d_batch* b, int* fwd_ctas_per_sm, int* filter_minb) {
   return b->tuned ? 1 : 0;
 }
 
+int f3d_batch_set_tune(f3d_batch* b, int fwd_ctas_per_sm, int filter_minb) {
+  if (!b) return fail_thread(F3D_E_PARAM, "FFT3DCL: null batch");
+  if (fwd_ctas_per_sm < 1 || fwd_ctas_per_sm > 2 || filter_minb < 3 || filter_minb > 5)
+    return batch_fail(b, F3D_E_PARAM, "FFT3DCL: unsupported launch shape");
+  cudaSetDevice(b->eng[0]->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  // Graphs captured with the previous shape are rebuilt at their next step.
+  for (auto& kv : b->graphs) {
+    if (kv.second.x) cudaGraphExecDestroy(kv.second.x);
+    if (kv.second.g) cudaGraphDestroy(kv.second.g);
+  }
+  b->graphs.clear();
+  b->tune = TcTune{fwd_ctas_per_sm, filter_minb};
+  b->tuned = true;
+  return F3D_OK;
+}
+
 }  // extern "C"
 

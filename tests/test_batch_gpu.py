@@ -11,9 +11,10 @@ from fft3dcl_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def run_planes(planes, params, chroma_flags, bits, batch_flags, ahead=False):
+def run_planes(planes, params, chroma_flags, bits, batch_flags, ahead=False, shape=None):
     """planes[i]: list of frames of plane i. Returns outputs per plane, by
-    the batch when batch_flags is not None, else by separate engines."""
+    the batch when batch_flags is not None (with the launch shape pinned to
+    `shape` when given), else by separate engines."""
     dev = torch.device("cuda", 0)
     st = torch.cuda.Stream(device=dev)
     nfr = len(planes[0])
@@ -26,6 +27,8 @@ def run_planes(planes, params, chroma_flags, bits, batch_flags, ahead=False):
     outs = [[] for _ in planes]
     pitch = [p[0].shape[1] * p[0].itemsize for p in planes]
     b = F.Batch(engines, graph=bool(batch_flags & 1), autotune=bool(batch_flags & 2)) if batch_flags is not None else None
+    if b is not None and shape is not None:
+        b.set_tune(*shape)
     with torch.cuda.stream(st):
         for n in range(nfr):
             win = [min(max(n - cur + i, 0), nfr - 1) for i in range(bt)]
@@ -93,6 +96,35 @@ def test_yuv_planes_batch_equals_engines(flags):
             np.testing.assert_array_equal(g, r, err_msg=f"plane {i} frame {n}")
     if flags & 2:
         assert tune["tuned"] and tune["fwd_ctas_per_sm"] in (1, 2) and tune["filter_minb"] in (3, 4, 5)
+
+
+@pytest.mark.parametrize("bt", [-1, 1, 2, 3, 4])
+def test_every_launch_shape_equals_engines(bt):
+    # Every filter-kernel variant (5, 4, 3 CTAs per SM) and forward grid (1,
+    # 2 CTAs per SM): the same bits as the engines, in every temporal mode.
+    planes = yuv420(400, 240, 6, 31 + bt, 10)[:2]
+    params = dict(sigma=3.0, bt=bt, sharpen=0.3, degrid=1.0)
+    ref, _ = run_planes(planes, params, [False, True], 10, None)
+    for shape in [(2, 5), (1, 5), (2, 4), (1, 3)]:
+        got, tune = run_planes(planes, params, [False, True], 10, 1, shape=shape)
+        assert (tune["fwd_ctas_per_sm"], tune["filter_minb"]) == shape
+        for i in range(2):
+            for n, (g, r) in enumerate(zip(got[i], ref[i])):
+                np.testing.assert_array_equal(g, r, err_msg=f"shape {shape} plane {i} frame {n}")
+
+
+def test_set_tune_rejects_unknown_shapes():
+    eng = F.Engine(128, 96, 8, form="tc", bt=3)
+    b = F.Batch([eng])
+    try:
+        for shape in [(3, 5), (0, 5), (2, 2), (2, 6)]:
+            with pytest.raises(F.F3DError):
+                b.set_tune(*shape)
+        b.set_tune(1, 3)
+        assert b.tune() == {"tuned": True, "fwd_ctas_per_sm": 1, "filter_minb": 3}
+    finally:
+        b.close()
+        eng.close()
 
 
 @pytest.mark.parametrize("flags", [0, 1])
