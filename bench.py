@@ -570,7 +570,7 @@ def main():
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
     ap.add_argument("--no-batch", action="store_true",
                     help="tensor-core headline through the engine's own calls instead of a batch step")
-    ap.add_argument("--outputs-per-step", type=int, default=2, choices=[1, 2, 3, 4],
+    ap.add_argument("--outputs-per-step", type=int, default=4, choices=[1, 2, 3, 4],
                     help="tensor-core batch: consecutive output frames per step")
     ap.add_argument("--size", default=None,
                     help="WxH of the luma plane instead of 3840x2160 (small cases for profiling)")

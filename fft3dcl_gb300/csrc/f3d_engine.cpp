@@ -76,6 +76,7 @@ struct f3d_engine {
 
   std::map<int, float2*> cache;
   std::vector<float2*> pool;
+  int pool_min = 2;  // spectra the retire pool keeps whatever the budget: a batch raises it to its outputs per step
 
   uint8_t* d_in = nullptr;   // raw or float plane, width*height*4 bytes
   uint8_t* d_out = nullptr;  // packed or float output plane
@@ -175,10 +176,11 @@ float2* spectra_slot(f3d_engine* e, int fn, bool create) {
 }
 
 // GpuRef::retireSpectra (src/cl/gpu.cpp:289-306): keep recycled buffers up
-// to 256 MiB, release the rest; at least two are kept, so that steps that
-// enter two frames (two outputs per batch step) do not allocate every time.
+// to 256 MiB, release the rest; at least pool_min are kept (two, or the
+// outputs per step of a batch the engine is in), so that steps that enter
+// several frames do not allocate every time.
 void retire(f3d_engine* e, float2* m) {
-  const size_t budget = std::max(size_t(256) << 20, 2 * e->spec_bytes);
+  const size_t budget = std::max(size_t(256) << 20, (size_t)e->pool_min * e->spec_bytes);
   if (e->pool.size() * e->spec_bytes + e->spec_bytes <= budget)
     e->pool.push_back(m);
   else
@@ -820,6 +822,13 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
   b->img_bytes.assign(n, 0);
   b->seam_bytes.assign(n, 0);
   for (int i = 0; i < n; i++) {
+    // An engine that appears k times enters k frames per step.
+    int k = 0;
+    for (int j = 0; j < n; j++) k += engines[j] == engines[i];
+    {
+      std::lock_guard<std::mutex> lk(engines[i]->mtx);
+      engines[i]->pool_min = std::max(engines[i]->pool_min, k);
+    }
     bool repeat = false;
     for (int j = 0; j < i; j++) repeat |= engines[j] == engines[i];
     if (!repeat) continue;

@@ -158,33 +158,36 @@ def test_batch_rejects_mixed_forms():
 
 
 @pytest.mark.parametrize("graph", [False, True])
-def test_two_outputs_per_step_equal_engine(graph):
-    # The same engine twice in a batch: two consecutive outputs per step, the
-    # forwards of the next two frames concurrent with them.
-    frames = synth.moving_rects(320, 192, 11, 51, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
+@pytest.mark.parametrize("k", [2, 4])
+def test_several_outputs_per_step_equal_engine(k, graph):
+    # The same engine k times in a batch: k consecutive outputs per step, the
+    # forwards of the next k frames concurrent with them.
+    frames = synth.moving_rects(320, 192, 13, 51, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
     params = dict(sigma=3.0, bt=4, sharpen=0.3)
     ref = F.FFT3DCL(frames, bits=10, form="tc", **params)
     dev = torch.device("cuda", 0)
     st = torch.cuda.Stream(device=dev)
     e = F.Engine(320, 192, 10, form="tc", stream=st.cuda_stream, **params)
     src = torch.from_numpy(np.stack(frames)).to(dev)
-    dst = [torch.empty((192, 320), dtype=torch.uint16, device=dev) for _ in range(2)]
-    b = F.Batch([e, e], graph=graph, autotune=True)
+    dst = [torch.empty((192, 320), dtype=torch.uint16, device=dev) for _ in range(k)]
+    b = F.Batch([e] * k, graph=graph, autotune=True)
     nfr, pitch = len(frames), 320 * 2
     got = []
     with torch.cuda.stream(st):
-        for n in range(0, nfr, 2):
-            wins = [[min(max(m - 2 + i, 0), nfr - 1) for i in range(4)] for m in (n, n + 1)]
+        for n in range(0, nfr, k):
+            wins = [[min(max(m - 2 + i, 0), nfr - 1) for i in range(4)] for m in range(n, n + k)]
             for w in wins:
                 for fn in w:
                     if not e.has(fn):
                         e.forward_device(fn, src[fn].data_ptr(), pitch)
-            ahead = [min(n + 3, nfr - 1), min(n + 4, nfr - 1)]
-            b.step(ahead, [src[a].data_ptr() for a in ahead], [pitch] * 2, wins,
-                   [d.data_ptr() for d in dst], [pitch] * 2)
+            # The frames after the last window, unless a clamped window holds them.
+            ahead = [n + k + 1 + i for i in range(k)]
+            ahead = [a if a < nfr else -1 for a in ahead]
+            b.step(ahead, [src[min(a, nfr - 1)].data_ptr() for a in ahead], [pitch] * k, wins,
+                   [d.data_ptr() for d in dst], [pitch] * k)
             st.synchronize()
-            got += [dst[0].cpu().numpy(), dst[1].cpu().numpy()]
-            e.prune(n - 3, n + 5)
+            got += [d.cpu().numpy() for d in dst]
+            e.prune(n - 3, n + 2 * k + 1)
     b.close()
     e.close()
     for n in range(nfr):
