@@ -3,9 +3,11 @@
 
 Workload: 3840x2160 10-bit luma, sigma=3 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4
 precision=2, a seeded synthetic 48-frame clip (ramp + moving rectangles in
-64..940, Gaussian noise 12 LSB). One step is one output frame in steady
-state: the forward transform of the frame that enters the temporal window,
-then filter + inverse + overlap-add + 10-bit packing of the current frame.
+64..940, Gaussian noise 12 LSB). One step of the tensor-core headline is one
+batch step of --outputs-per-step (default 4) consecutive output frames in
+steady state: the forward transforms of the frames that enter the temporal
+window, then filter + inverse + overlap-add + 10-bit packing of each output.
+The other forms run one output frame per step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--form exact|fast|tc]
     python bench.py --impl reference ...   # the reference CPU path on the host cores
@@ -570,7 +572,7 @@ def main():
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
     ap.add_argument("--no-batch", action="store_true",
                     help="tensor-core headline through the engine's own calls instead of a batch step")
-    ap.add_argument("--outputs-per-step", type=int, default=4, choices=[1, 2, 3, 4],
+    ap.add_argument("--outputs-per-step", type=int, default=4, choices=list(range(1, 9)),
                     help="tensor-core batch: consecutive output frames per step")
     ap.add_argument("--size", default=None,
                     help="WxH of the luma plane instead of 3840x2160 (small cases for profiling)")

@@ -584,8 +584,9 @@ BATCH_AUTOTUNE = 2
 
 
 class Batch:
-    """One temporal step of up to four tensor-core engines (the planes of a
-    frame, or planes of several streams) with one launch per kernel
+    """One temporal step of up to eight tensor-core engines (the planes of a
+    frame, planes of several streams, or one engine several times for
+    consecutive outputs) with one launch per kernel
     (f3d_batch_*); optionally replayed as a CUDA graph and autotuned."""
 
     def __init__(self, engines: list, graph: bool = True, autotune: bool = True):

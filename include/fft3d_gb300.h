@@ -233,8 +233,9 @@ int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
                         size_t dst_pitch, void* stream);
 
 /* ---- Batches of planes -----------------------------------------------------
- * One temporal step of up to four planes (the planes of a YUV frame, or
- * planes of several streams) with one launch per kernel: the forward
+ * One temporal step of up to eight planes (the planes of a YUV frame,
+ * planes of several streams, or consecutive outputs of one plane: the same
+ * engine given several times) with one launch per kernel: the forward
  * transform of each plane's entering frame, then filter, inverse and
  * overlap-add of each plane's window. The engines must run the fused
  * tensor-core form (F3D_FORM_TC, half overlap, 32x32 blocks) on one device

@@ -158,7 +158,7 @@ def test_batch_rejects_mixed_forms():
 
 
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("k", [2, 4])
+@pytest.mark.parametrize("k", [2, 4, 8])
 def test_several_outputs_per_step_equal_engine(k, graph):
     # The same engine k times in a batch: k consecutive outputs per step, the
     # forwards of the next k frames concurrent with them.
