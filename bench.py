@@ -192,10 +192,14 @@ def yuv_batched(args, dev, local_rank):
     ip = F.validate(w, h, 8, **YUV_PARAMS)
     bt, cur = ip.bt, ip.current
     res = {}
-    for form in ("tc", "fast"):
+    for name in ("tc", "tc_half", "fast"):
+        form = "fast" if name == "fast" else "tc"
+        flags = F.FLAG_HALF_SPECTRA if name == "tc_half" else 0
         st = torch.cuda.Stream(device=dev)
         engs = [F.Engine(p[0].shape[1], p[0].shape[0], 8, chroma=i > 0, form=form, device=local_rank,
-                         stream=st.cuda_stream, **YUV_PARAMS) for i, p in enumerate(planes)]
+                         stream=st.cuda_stream, flags=flags, **YUV_PARAMS) for i, p in enumerate(planes)]
+        if flags:
+            assert all(e.info().half_spectra for e in engs)
         batch = F.Batch(engs, graph=True, autotune=True) if form == "tc" else None
 
         def step(n):
@@ -232,15 +236,17 @@ def yuv_batched(args, dev, local_rank):
         e1.record(st)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
-        res[form] = {"frames_per_s": round(args.steps / (ms / 1000.0), 1),
+        res[name] = {"frames_per_s": round(args.steps / (ms / 1000.0), 1),
                      "launches_per_frame": round((F.kernel_launches() - l0) / args.steps, 2)}
         if batch is not None:
-            res[form]["tune"] = batch.tune()
+            res[name]["tune"] = batch.tune()
             batch.close()
         for e in engs:
             e.close()
     res["tc"]["form"] = ("tensor cores, 3 planes per launch, CUDA graph per frame, forward one frame ahead "
                          "concurrent with the outputs")
+    res["tc_half"]["form"] = ("as tc, spectra cached as fp16 pairs (F3D_FLAG_HALF_SPECTRA: the original's "
+                              "storage at precision 0, the default; opt-in, within +-1 LSB of the fp32 path)")
     res["fast"]["form"] = "fp32 radix FFT, per-plane engines"
     return res
 

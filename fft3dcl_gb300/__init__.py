@@ -78,7 +78,7 @@ class Options(C.Structure):
     _fields_ = [("device", C.c_int), ("form", C.c_int), ("stream", C.c_void_p), ("flags", C.c_int)]
 
 
-FLAG_UNFUSED, FLAG_PREFETCH_EARLY, FLAG_PREFETCH_LATE = 1, 2, 4
+FLAG_UNFUSED, FLAG_PREFETCH_EARLY, FLAG_PREFETCH_LATE, FLAG_HALF_SPECTRA = 1, 2, 4, 8
 
 
 class EngineInfo(C.Structure):
@@ -86,7 +86,7 @@ class EngineInfo(C.Structure):
                 ("bytes_per_sample", C.c_int), ("raw_path", C.c_int),
                 ("spectrum_bytes", C.c_size_t), ("device_bytes", C.c_size_t),
                 ("cached_frames", C.c_int), ("chroma_norm", C.c_float), ("form", C.c_int),
-                ("fused", C.c_int)]
+                ("fused", C.c_int), ("half_spectra", C.c_int)]
 
 
 # Every symbol the C ABI declares (include/fft3d_gb300.h).
@@ -409,7 +409,7 @@ class Filter:
     order, as the reference's fmFrameState mode delivers them."""
 
     def __init__(self, clip, fmt: VideoFormat, form: str = "exact", device: int = 2,
-                 gpu: int = 0, fused: bool = True, **params):
+                 gpu: int = 0, fused: bool = True, flags: int = 0, **params):
         if fmt.sample_type == 1 and fmt.bits != 32:
             raise ValueError("FFT3DCL: only 32-bit float clips supported (16-bit float not ported yet)")
         if fmt.sample_type == 0 and not 8 <= fmt.bits <= 16:
@@ -446,7 +446,7 @@ class Filter:
                 h, w = first[p].shape
                 self.engines.append(Engine(w, h, fmt.bits, fmt.sample_type,
                                            chroma=(fmt.color_family == "yuv" and p > 0),
-                                           form=form, device=gpu, fused=fused, **params))
+                                           form=form, device=gpu, fused=fused, flags=flags, **params))
         except Exception:
             self.close()
             raise

@@ -12,6 +12,7 @@
 #include "f3d_host.hpp"
 #include "f3d_kernels.hpp"
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -77,6 +78,7 @@ struct f3d_engine {
   std::map<int, float2*> cache;
   std::vector<float2*> pool;
   int pool_min = 2;  // spectra the retire pool keeps whatever the budget: a batch raises it to its outputs per step
+  bool half = false; // spectra stored as fp16 pairs (F3D_FLAG_HALF_SPECTRA applied)
 
   uint8_t* d_in = nullptr;   // raw or float plane, width*height*4 bytes
   uint8_t* d_out = nullptr;  // packed or float output plane
@@ -200,6 +202,7 @@ TcFwdArgs tc_forward_args(const f3d_engine* e, const uint8_t* dsrc, long long pi
   t.chroma_norm = e->cnorm;
   t.tab = e->d_tc;
   t.spec = spec;
+  t.half = e->half ? 1 : 0;
   t.err = e->d_err;
   return t;
 }
@@ -250,6 +253,7 @@ int inverse_args(f3d_engine* e, const int* window, int n, InvArgs& a) {
   if (e->ip.degrid_on && !e->degrid_active) e->degrid_active = true;
   a.g = make_geo(e);
   a.tw = make_twiddles(e);
+  a.half = e->half ? 1 : 0;
   a.cur = e->ip.bm >= 2 ? e->ip.current : 0;
   a.bm = e->ip.bm;
   a.dg = e->ip.degrid_on && e->degrid_active;
@@ -528,6 +532,11 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
     e->fused = true;
     const int fl = opts ? opts->flags : 0;
     e->sweep_prefetch = (fl & F3D_FLAG_PREFETCH_EARLY) ? 1 : (fl & F3D_FLAG_PREFETCH_LATE) ? 2 : 0;
+    // Half storage where the original filter used it (8-bit, precision 0/1)
+    // and the tensor-core kernels read and write it.
+    e->half = (fl & F3D_FLAG_HALF_SPECTRA) && e->form == F3D_FORM_TC && e->inv_form == F3D_FORM_TC &&
+              e->fmt == FMT_U8 && ip.precision < 2;
+    if (e->half) e->spec_bytes = sizeof(__half2) * (size_t)e->grid.nb * e->ps;
   }
   // The windowed-block buffer of the separate inverse and overlap-add kernels.
   if (!e->fused && (ce = e->alloc(&e->d_blocks, sizeof(float) * bwbh * e->grid.nb)) != cudaSuccess)
@@ -588,6 +597,7 @@ int f3d_engine_get_info(f3d_engine* e, f3d_engine_info* info) {
   info->chroma_norm = e->cnorm;
   info->form = e->form;
   info->fused = e->fused ? 1 : 0;
+  info->half_spectra = e->half ? 1 : 0;
   return F3D_OK;
 }
 
@@ -645,6 +655,18 @@ int f3d_get_spectra(f3d_engine* e, int fn, float* dst) {
   Lock l(e);
   const float2* s = spectra_slot(e, fn, false);
   if (!s) return e->fail(F3D_E_STATE, "FFT3DCL: frame " + std::to_string(fn) + " is not cached");
+  if (e->half) {
+    // fp16 pairs, widened to float on the host.
+    std::vector<__half2> h(e->spec_bytes / sizeof(__half2));
+    cudaError_t ce = cudaMemcpyAsync(h.data(), s, e->spec_bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return e->cuda_fail(ce, "spectra readback");
+    for (size_t i = 0; i < h.size(); i++) {
+      dst[2 * i] = __low2float(h[i]);
+      dst[2 * i + 1] = __high2float(h[i]);
+    }
+    return F3D_OK;
+  }
   cudaError_t ce = cudaMemcpyAsync(dst, s, e->spec_bytes, cudaMemcpyDeviceToHost, e->stream);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
   if (ce != cudaSuccess) return e->cuda_fail(ce, "spectra readback");
@@ -808,9 +830,9 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
     if (e->device != e0->device || e->stream != e0->stream)
       return fail_thread(F3D_E_PARAM, "FFT3DCL: the engines of a batch share one device and stream");
     if (e->ip.bw != e0->ip.bw || e->ip.bh != e0->ip.bh || e->ip.ow != e0->ip.ow || e->ip.oh != e0->ip.oh ||
-        e->ip.wintype != e0->ip.wintype || e->ip.bm != e0->ip.bm || e->fmt != e0->fmt)
-      return fail_thread(F3D_E_UNSUPPORTED,
-                         "FFT3DCL: the planes of a batch share block size, overlap, window, temporal mode and format");
+        e->ip.wintype != e0->ip.wintype || e->ip.bm != e0->ip.bm || e->fmt != e0->fmt || e->half != e0->half)
+      return fail_thread(F3D_E_UNSUPPORTED, "FFT3DCL: the planes of a batch share block size, overlap, window, "
+                                            "temporal mode, format and spectrum storage");
   }
   auto* b = new f3d_batch();
   b->eng.assign(engines, engines + n);

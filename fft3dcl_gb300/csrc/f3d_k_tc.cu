@@ -389,12 +389,29 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
         }
       }
     }
+    // Half storage: the staged spectra narrowed to fp16 pairs in place (all
+    // values read before any is written).
+    if (a.half) {
+      constexpr int PER = C::G * C::PS / kTcThreads;
+      static_assert(C::G * C::PS % kTcThreads == 0, "staged values per thread");
+      float2 r[PER];
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < PER; i++) r[i] = stage[tid + kTcThreads * i];
+      __syncthreads();
+      __half2* hs = reinterpret_cast<__half2*>(stage);
+#pragma unroll
+      for (int i = 0; i < PER; i++) hs[tid + kTcThreads * i] = __float22half2_rn(r[i]);
+    }
     tc::fence_async_smem();
     __syncthreads();
 
     // 8. One bulk copy of the group's spectra to HBM.
     if (tid == 0 && nvalid > 0) {
-      tc::bulk_store(a.spec + (size_t)b0 * C::PS, stage, (uint32_t)(nvalid * C::PS * 8));
+      if (a.half)
+        tc::bulk_store(reinterpret_cast<__half2*>(a.spec) + (size_t)b0 * C::PS, stage, (uint32_t)(nvalid * C::PS * 4));
+      else
+        tc::bulk_store(a.spec + (size_t)b0 * C::PS, stage, (uint32_t)(nvalid * C::PS * 8));
       tc::bulk_commit();
     }
   }
@@ -499,7 +516,14 @@ __device__ __forceinline__ void emit16(const SweepArgs& sa, int y, int x0, const
   }
 }
 
-template <int N, int BM, int MINB>
+// Bin j of a spectrum stored as float2 or, with half storage, as __half2.
+template <bool HALF>
+__device__ __forceinline__ float2 spec_at(const float2* s, size_t j) {
+  if constexpr (HALF) return __half22float2(reinterpret_cast<const __half2*>(s)[j]);
+  else return s[j];
+}
+
+template <int N, int BM, int MINB, bool HALF>
 __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_constant__ SweepBatch B) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
@@ -532,11 +556,14 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
   // The group's window spectra start moving into L2 as whole runs, so that
   // the bins' loads below mostly wait on L2 rather than on DRAM.
+  constexpr uint32_t BIN_BYTES = HALF ? 4 : 8;
   if (F3D_TC_FILTER_PREFETCH && tid < NF && nvbin > 0)
-    tc::prefetch_l2(a.s[tid] + gb0, (uint32_t)(nvbin * sizeof(float2)));
+    tc::prefetch_l2(reinterpret_cast<const uint8_t*>(a.s[tid]) + gb0 * BIN_BYTES, (uint32_t)(nvbin * BIN_BYTES));
   if (tid < C::G) {
     const int n = J0 + tid;
-    dcs[tid] = (n <= sa.cells_x && n < ncols) ? block_dc(a, m * ncols + n) : 0.0f;
+    dcs[tid] = (a.dg && n <= sa.cells_x && n < ncols)
+                   ? spec_at<HALF>(a.s[a.cur], (size_t)(m * ncols + n) * C::PS).x
+                   : 0.0f;
   }
   __syncthreads();
 
@@ -546,7 +573,8 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   // further (constant offsets).
   const float2* sp[NF];
 #pragma unroll
-  for (int k = 0; k < NF; k++) sp[k] = a.s[k] + gb0 + tid;
+  for (int k = 0; k < NF; k++) sp[k] = a.s[k];
+  const size_t b0i = gb0 + tid;
 #pragma unroll
   for (int j0 = 0; j0 < NB; j0 += kTcFilterBatch) {
     float2 sv[kTcFilterBatch][4];
@@ -555,7 +583,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
       const int i = tid + kTcThreads * (j0 + u);
       if (j0 + u < NB && i < nvbin) {
 #pragma unroll
-        for (int k = 0; k < NF; k++) sv[u][k] = sp[k][kTcThreads * (j0 + u)];
+        for (int k = 0; k < NF; k++) sv[u][k] = spec_at<HALF>(sp[k], b0i + kTcThreads * (j0 + u));
       }
     }
 #pragma unroll
@@ -968,7 +996,8 @@ bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& B
   B.n = n;
   for (int i = 0; i < n; i++) {
     const SweepArgs& a = planes[i];
-    if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm)
+    if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm ||
+        a.inv.half != planes[0].inv.half)
       return false;
     B.p[i] = a;
   }
@@ -1013,10 +1042,10 @@ cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune
 
 cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st) { return launch_forward_tc_batch(&a, 1, TcTune{}, st); }
 
-template <int BM, int MINB>
+template <int BM, int MINB, bool HALF>
 cudaError_t launch_filter_bm(const SweepBatch& B, cudaStream_t st) {
   constexpr size_t smem = SwpCfg<32>::F_BYTES;
-  auto k = k_filter_tc<32, BM, MINB>;
+  auto k = k_filter_tc<32, BM, MINB, HALF>;
   cudaError_t e = prepare(k, smem);
   if (e != cudaSuccess) return e;
   if (B.cta0[B.n] == 0) return cudaSuccess;
@@ -1025,16 +1054,22 @@ cudaError_t launch_filter_bm(const SweepBatch& B, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int MINB>
-cudaError_t launch_filter(const SweepBatch& B, int bm, cudaStream_t st) {
+template <int MINB, bool HALF>
+cudaError_t launch_filter_h(const SweepBatch& B, int bm, cudaStream_t st) {
   switch (bm) {
-  case -1: return launch_filter_bm<-1, MINB>(B, st);
-  case 1: return launch_filter_bm<1, MINB>(B, st);
-  case 2: return launch_filter_bm<2, MINB>(B, st);
-  case 3: return launch_filter_bm<3, MINB>(B, st);
-  case 4: return launch_filter_bm<4, MINB>(B, st);
+  case -1: return launch_filter_bm<-1, MINB, HALF>(B, st);
+  case 1: return launch_filter_bm<1, MINB, HALF>(B, st);
+  case 2: return launch_filter_bm<2, MINB, HALF>(B, st);
+  case 3: return launch_filter_bm<3, MINB, HALF>(B, st);
+  case 4: return launch_filter_bm<4, MINB, HALF>(B, st);
   default: return cudaErrorNotSupported;
   }
+}
+
+// The planes of a batch share the spectrum storage (sweep_batches checks).
+template <int MINB>
+cudaError_t launch_filter(const SweepBatch& B, int bm, cudaStream_t st) {
+  return B.p[0].inv.half ? launch_filter_h<MINB, true>(B, bm, st) : launch_filter_h<MINB, false>(B, bm, st);
 }
 
 // Finishes the seam cell rows of every plane of the batch: blockIdx.z runs
@@ -1095,11 +1130,15 @@ cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mar
 }
 
 namespace {
+template <int MINB, bool HALF>
+bool is_filter_h(const void* f) {
+  return f == (const void*)k_filter_tc<32, -1, MINB, HALF> || f == (const void*)k_filter_tc<32, 1, MINB, HALF> ||
+         f == (const void*)k_filter_tc<32, 2, MINB, HALF> || f == (const void*)k_filter_tc<32, 3, MINB, HALF> ||
+         f == (const void*)k_filter_tc<32, 4, MINB, HALF>;
+}
 template <int MINB>
 bool is_filter(const void* f) {
-  return f == (const void*)k_filter_tc<32, -1, MINB> || f == (const void*)k_filter_tc<32, 1, MINB> ||
-         f == (const void*)k_filter_tc<32, 2, MINB> || f == (const void*)k_filter_tc<32, 3, MINB> ||
-         f == (const void*)k_filter_tc<32, 4, MINB>;
+  return is_filter_h<MINB, false>(f) || is_filter_h<MINB, true>(f);
 }
 }  // namespace
 

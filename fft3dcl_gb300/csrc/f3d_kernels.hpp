@@ -45,7 +45,8 @@ struct FwdArgs {
 struct InvArgs {
   Geo g;
   Twiddles tw;
-  const float2* s[4];  // window spectra in temporal order
+  const float2* s[4];  // window spectra in temporal order (__half2 pairs when half)
+  int half;            // spectra stored as fp16 pairs (tensor-core filter only)
   int cur;             // index of the current frame in s
   int bm;              // temporal mode -1..4
   int dg, pat, shp;    // degrid, sigma pattern, sharpen on
@@ -140,7 +141,8 @@ struct TcFwdArgs {
   float out_scale;     // applied to the spectra: 1/255 or norm on the integer path, 1 on the split path
   float chroma_norm;
   const uint8_t* tab;  // device copy of tc_tables()
-  float2* spec;        // out: nb x bh x fbw half spectra
+  float2* spec;        // out: nb x bh x fbw half spectra (__half2 pairs when half)
+  int half;            // store the spectra as fp16 pairs
   int* err;            // set non-zero when a tensor-core wait gives up
 };
 bool tc_supported(int mode, int bw, int bh, int bm);

@@ -102,6 +102,17 @@ typedef struct {
  * at 4K 10-bit bt=4: off 0.288 ms, late 0.292 ms, early 0.322 ms). */
 #define F3D_FLAG_PREFETCH_EARLY 2
 #define F3D_FLAG_PREFETCH_LATE 4
+/* Cache the spectra as fp16 pairs (half the bytes: the forward writes half
+ * as much, the filter reads half as much), the storage of the original
+ * filter's precision 0 and 1: its FFT returns spectra in HALF4 textures
+ * unless precision is FLOAT32_ALL (upstream/FFT3dGPU/FFT.cpp:152), which is
+ * forced above 8 bits (upstream/FFT3dGPU/FFT3dGPU.cpp:244-246; the port's
+ * src/params.h:116-120). Honoured where that storage applied and the kernels take it: 8-bit
+ * integer planes, precision 0 or 1, the fused tensor-core form; ignored
+ * elsewhere (f3d_engine_info.half_spectra says which). Arithmetic stays
+ * fp32; results are within the 8-bit tolerance of the fp32 path, not
+ * bit-equal to it. The reference port ignores precision, so this is opt-in. */
+#define F3D_FLAG_HALF_SPECTRA 8
 
 typedef struct {
   int nblocks, fbw, ncols, nrows;
@@ -114,6 +125,7 @@ typedef struct {
   int form; /* form the engine runs: Kalman (bt=0) and 4-wide blocks run
                F3D_FORM_EXACT whatever was asked */
   int fused; /* filter, inverse, overlap-add and packing run as one kernel */
+  int half_spectra; /* spectra cached as fp16 pairs (F3D_FLAG_HALF_SPECTRA applied) */
 } f3d_engine_info;
 
 typedef struct f3d_engine f3d_engine;
