@@ -1,6 +1,6 @@
 """Command-line driver: denoise a .y4m clip with the GB300 engine.
 
-    python -m fft3dcl_gb300 IN.y4m OUT.y4m [--form exact|fast|tc] [--gpu N]
+    python -m fft3dcl_gb300 IN.y4m OUT.y4m [--form exact|fast|tc] [--gpu N] [--half-spectra]
         [--sigma S --bt N --bw N --bh N --ow N --oh N --sharpen X --plane P ...]
 
 Every FFT3DCL argument of the plugin (src/fft3dcl.cpp:540-546) is accepted as
@@ -13,7 +13,7 @@ import argparse
 import sys
 import time
 
-from . import Filter, VideoFormat, ScriptParams
+from . import FLAG_HALF_SPECTRA, Filter, VideoFormat, ScriptParams
 from .y4m import Y4MClip, Y4MWriter
 
 _INT = {"bw", "bh", "bt", "plane", "mode", "bordersize", "precision", "ow", "oh", "wintype", "interlaced", "oldfft"}
@@ -26,6 +26,8 @@ def main(argv=None) -> int:
     ap.add_argument("--form", default="tc", choices=["exact", "fast", "tc"])
     ap.add_argument("--gpu", type=int, default=0)
     ap.add_argument("--frames", type=int, default=0, help="process only the first N frames")
+    ap.add_argument("--half-spectra", action="store_true",
+                    help="cache the spectra as fp16 (8-bit clips at precision 0/1, tensor-core form)")
     for name, _ in ScriptParams._fields_:
         ap.add_argument(f"--{name}", type=int if name in _INT else float, default=None)
     args = ap.parse_args(argv)
@@ -34,7 +36,8 @@ def main(argv=None) -> int:
         n = len(clip) if args.frames <= 0 else min(args.frames, len(clip))
         fmt = VideoFormat("gray" if clip.mono else "yuv", clip.bits, 0, clip.sub_w, clip.sub_h)
         view = _Prefix(clip, n)
-        flt = Filter(view, fmt, form=args.form, gpu=args.gpu, **params)
+        flt = Filter(view, fmt, form=args.form, gpu=args.gpu,
+                     flags=FLAG_HALF_SPECTRA if args.half_spectra else 0, **params)
         t0 = time.perf_counter()
         try:
             with Y4MWriter(args.output, header=clip.header) as out:

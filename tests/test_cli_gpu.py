@@ -29,3 +29,24 @@ def test_cli_matches_filter(tmp_path, bits, form):
         for n in range(len(frames)):
             for a, b in zip(out[n], ref[n]):
                 np.testing.assert_array_equal(a, b)
+
+
+def test_cli_half_spectra_matches_filter(tmp_path):
+    frames = clip420(160, 96, 5, 8, seed=19)
+    src, dst = tmp_path / "in.y4m", tmp_path / "out.y4m"
+    with Y4MWriter(str(src), width=160, height=96, bits=8) as w:
+        for f in frames:
+            w.write(f)
+    assert cli.main([str(src), str(dst), "--form", "tc", "--plane", "4", "--bt", "3", "--precision", "0",
+                     "--half-spectra"]) == 0
+    flt = F.Filter(frames, F.VideoFormat("yuv", 8, 0, 1, 1), form="tc", plane=4, bt=3, precision=0,
+                   flags=F.FLAG_HALF_SPECTRA)
+    try:
+        assert all(e.info().half_spectra for e in flt.engines)
+        ref = [flt.get_frame(n) for n in range(len(frames))]
+    finally:
+        flt.close()
+    with Y4MClip(str(dst)) as out:
+        for n in range(len(frames)):
+            for a, b in zip(out[n], ref[n]):
+                np.testing.assert_array_equal(a, b)
