@@ -276,6 +276,24 @@ def run_reference(args):
 
 # --------------------------------------------------------------- GPU leg --
 
+def slowest_rank(times_ms: list, world: int) -> list:
+    """Replicas: each timing taken as the maximum over the ranks (the job
+    ends when its slowest replica does), so that whole-job throughput is the
+    units all ranks processed divided by that time."""
+    if world <= 1:
+        return list(times_ms)
+    import torch
+    t = torch.tensor(times_ms, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def replica_throughput(units_per_rank: float, world: int, ms: float) -> float:
+    """Whole-job throughput of `world` replicas that each processed
+    units_per_rank units in at most ms milliseconds."""
+    return units_per_rank * world / (ms / 1000.0)
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     import fft3dcl_gb300 as F
@@ -479,14 +497,11 @@ def run_gpu(args, rank, world, local_rank):
         pbatch.close()
     eng.close()
 
-    if world > 1:
-        t = torch.tensor([ms, ms_e2e], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ms_e2e = float(t[0]), float(t[1])
+    ms, ms_e2e = slowest_rank([ms, ms_e2e], world)
     if rank != 0:
         return
-    fps = args.steps * kframes * world / (ms / 1000.0)
-    fps_e2e = args.steps * kframes * world / (ms_e2e / 1000.0)
+    fps = replica_throughput(args.steps * kframes, world, ms)
+    fps_e2e = replica_throughput(args.steps * kframes, world, ms_e2e)
     ab = algorithmic_bytes(info.nblocks, info.fbw, ip.bh, bt)
     peak, peak_kind = load_peaks()
     inv_ms = float(kt[1])
