@@ -114,6 +114,15 @@ __device__ __forceinline__ void wienner_t(float& re, float& im, float sx, float 
   im *= mul;
 }
 
+// Fast forms, temporal modes 2-4: the Wiener gain of one temporal
+// frequency with the average's 1/bm folded in, s * max(1 - sy/psd, beta_x)
+// evaluated as max(s - (s sy)/psd, s beta_x) (exact for s = 1/2, 1/4), so that
+// the filtered value is a fused sum of gain x frequency.
+__device__ __forceinline__ float wiener_gain_scaled(float re, float im, float ssy, float s, float sbx) {
+  const float psd = fmaf(re, re, im * im);
+  return fmaxf(fmaf(-ssy, 1.0f / psd, s), sbx);
+}
+
 // Temporal mode as a template argument: -1..4 fixed at compile time (no
 // branch, and no Kalman state stores in the other modes' code, so the
 // compiler may move spectra loads freely), kRuntimeBm to read a.bm.
@@ -156,10 +165,17 @@ __device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i,
       br -= 2.0f * d_re;
       bi -= 2.0f * d_im;
     }
-    wienner_t<FAST>(ar, ai, sx, sy, a.beta_x);
-    wienner_t<FAST>(br, bi, sx, sy, a.beta_x);
-    fr = (ar + br) * 0.5f;
-    fi = (ai + bi) * 0.5f;
+    if (FAST) {
+      const float s = 0.5f, ssy = s * sy, sbx = s * a.beta_x;
+      const float ga = wiener_gain_scaled(ar, ai, ssy, s, sbx), gb = wiener_gain_scaled(br, bi, ssy, s, sbx);
+      fr = fmaf(gb, br, ga * ar);
+      fi = fmaf(gb, bi, ga * ai);
+    } else {
+      wienner(ar, ai, sx, sy, a.beta_x);
+      wienner(br, bi, sx, sy, a.beta_x);
+      fr = (ar + br) * 0.5f;
+      fi = (ai + bi) * 0.5f;
+    }
     if (a.dg) {
       fr += d_re;
       fi += d_im;
@@ -178,11 +194,19 @@ __device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i,
       d1r -= 3.0f * d_re;
       d1i -= 3.0f * d_im;
     }
-    wienner_t<FAST>(d0r, d0i, sx, sy, a.beta_x);
-    wienner_t<FAST>(d1r, d1i, sx, sy, a.beta_x);
-    wienner_t<FAST>(d2r, d2i, sx, sy, a.beta_x);
-    fr = (d0r + d1r + d2r) * (1.0f / 3.0f);
-    fi = (d0i + d1i + d2i) * (1.0f / 3.0f);
+    if (FAST) {
+      const float s = 1.0f / 3.0f, ssy = s * sy, sbx = s * a.beta_x;
+      const float g0 = wiener_gain_scaled(d0r, d0i, ssy, s, sbx), g1 = wiener_gain_scaled(d1r, d1i, ssy, s, sbx);
+      const float g2 = wiener_gain_scaled(d2r, d2i, ssy, s, sbx);
+      fr = fmaf(g2, d2r, fmaf(g1, d1r, g0 * d0r));
+      fi = fmaf(g2, d2i, fmaf(g1, d1i, g0 * d0i));
+    } else {
+      wienner(d0r, d0i, sx, sy, a.beta_x);
+      wienner(d1r, d1i, sx, sy, a.beta_x);
+      wienner(d2r, d2i, sx, sy, a.beta_x);
+      fr = (d0r + d1r + d2r) * (1.0f / 3.0f);
+      fi = (d0i + d1i + d2i) * (1.0f / 3.0f);
+    }
     if (a.dg) {
       fr += d_re;
       fi += d_im;
@@ -209,12 +233,20 @@ __device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i,
       fp1r -= 4.0f * d_re;
       fp1i -= 4.0f * d_im;
     }
-    wienner_t<FAST>(fp2r, fp2i, sx, sy, a.beta_x);
-    wienner_t<FAST>(fp1r, fp1i, sx, sy, a.beta_x);
-    wienner_t<FAST>(fcr, fci, sx, sy, a.beta_x);
-    wienner_t<FAST>(fnr, fni, sx, sy, a.beta_x);
-    fr = (fp2r + fp1r + fcr + fnr) * 0.25f;
-    fi = (fp2i + fp1i + fci + fni) * 0.25f;
+    if (FAST) {
+      const float s = 0.25f, ssy = s * sy, sbx = s * a.beta_x;
+      const float g2 = wiener_gain_scaled(fp2r, fp2i, ssy, s, sbx), g1 = wiener_gain_scaled(fp1r, fp1i, ssy, s, sbx);
+      const float gc = wiener_gain_scaled(fcr, fci, ssy, s, sbx), gn = wiener_gain_scaled(fnr, fni, ssy, s, sbx);
+      fr = fmaf(gn, fnr, fmaf(gc, fcr, fmaf(g1, fp1r, g2 * fp2r)));
+      fi = fmaf(gn, fni, fmaf(gc, fci, fmaf(g1, fp1i, g2 * fp2i)));
+    } else {
+      wienner(fp2r, fp2i, sx, sy, a.beta_x);
+      wienner(fp1r, fp1i, sx, sy, a.beta_x);
+      wienner(fcr, fci, sx, sy, a.beta_x);
+      wienner(fnr, fni, sx, sy, a.beta_x);
+      fr = (fp2r + fp1r + fcr + fnr) * 0.25f;
+      fi = (fp2i + fp1i + fci + fni) * 0.25f;
+    }
     if (a.dg) {
       fr += d_re;
       fi += d_im;
