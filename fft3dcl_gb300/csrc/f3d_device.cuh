@@ -214,11 +214,25 @@ __device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i,
   } else if (bm == 4) {
     const float2 p2 = sv[0], p1 = sv[1], c = sv[2], n = sv[3];
     float fp1r, fp1i, fcr, fci, fnr, fni, fp2r, fp2i;
-    if (FAST) {  // radix 2 x 2: (c +- p2), (p1 +- n)
+    if (FAST) {  // radix 2 x 2: (c +- p2), (p1 +- n), on (re, im) pairs
+#if __CUDA_ARCH__ >= 1000
+      // Packed fp32x2 adds; a - b as b * -1 + a, one rounding like the
+      // scalar subtraction, so the values equal the scalar form's.
+      const float2 m1 = make_float2(-1.0f, -1.0f);
+      const float2 s2 = __fadd2_rn(c, p2), d2 = __ffma2_rn(p2, m1, c);
+      const float2 t2 = __fadd2_rn(p1, n), e2 = __ffma2_rn(n, m1, p1);
+      const float2 fc2 = __fadd2_rn(s2, t2), fp22 = __ffma2_rn(t2, m1, s2);
+      const float2 es = make_float2(e2.y, e2.x);
+      const float2 fp12 = __ffma2_rn(es, make_float2(1.0f, -1.0f), d2);
+      const float2 fn2 = __ffma2_rn(es, make_float2(-1.0f, 1.0f), d2);
+      fcr = fc2.x, fci = fc2.y, fp2r = fp22.x, fp2i = fp22.y;
+      fp1r = fp12.x, fp1i = fp12.y, fnr = fn2.x, fni = fn2.y;
+#else
       const float sr = c.x + p2.x, si = c.y + p2.y, dr = c.x - p2.x, di = c.y - p2.y;
       const float tr = p1.x + n.x, ti = p1.y + n.y, er = p1.x - n.x, ei = p1.y - n.y;
       fcr = sr + tr, fci = si + ti, fp2r = sr - tr, fp2i = si - ti;
       fp1r = dr + ei, fp1i = di - er, fnr = dr - ei, fni = di + er;
+#endif
     } else {
       fp1r = -p2.x + p1.y + c.x - n.y;
       fp1i = -p2.y - p1.x + c.y + n.x;
