@@ -463,8 +463,11 @@ struct SwpCfg {
   static constexpr uint32_t C2 = 0;                                  // hi, lo
   static constexpr uint32_t C1 = C2 + 2 * C::B2_BYTES;               // A hi, A lo, B hi, B lo
   static constexpr uint32_t A2 = (C1 + 4 * C::B1_BYTES + 1023) / 1024 * 1024;  // hi, lo (SWIZZLE_128B)
-  static constexpr uint32_t A1 = A2 + TILE;                          // [tile][hi, lo] (INTERLEAVE)
-  static constexpr uint32_t P = A1 + 2 * C::T1 * C::A1_BYTES;        // [2][TJ][PC] floats
+  // A1 shares A2's space: step 2' has read the operand tile before V writes
+  // A1, and the next tile is loaded once step 1' has read A1. Three CTAs fit
+  // on an SM.
+  static constexpr uint32_t A1 = A2;                                 // [tile][hi, lo] (INTERLEAVE)
+  static constexpr uint32_t P = A2 + TILE;                           // [2][TJ][PC] floats
   static constexpr uint32_t BAR = P + 2 * TJ * PC * 4;               // operand load, step 2', step 1'
   static constexpr uint32_t TSLOT = BAR + 24;
   static constexpr uint32_t BYTES = TSLOT + 8 + 1024;
@@ -472,6 +475,7 @@ struct SwpCfg {
   static constexpr uint32_t F_DC = C::G * FS * 8;
   static constexpr uint32_t F_BYTES = F_DC + C::G * 4;
   static_assert(C::T1 == 2, "one tile per block-column parity");
+  static_assert(2 * C::T1 * C::A1_BYTES <= TILE, "A1 fits the operand tile's space");
   static_assert(BAR % 8 == 0 && P % 16 == 0, "alignment");
 };
 
@@ -638,7 +642,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
 }
 
 template <int N>
-__global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constant__ SweepBatch B) {
+__global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(const __grid_constant__ SweepBatch B) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
   using T = TcTab<N>;
@@ -718,11 +722,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
       break;
     }
     tc::fence_after_sync();
-    // The operand tile is consumed: the next row's starts moving in.
-    if (tid == 0 && m + 1 < M1) {
-      tc::mbar_expect_tx(&bar[0], S::TILE);
-      tc::bulk_load(sm + S::A2, tile_of(m + 1), S::TILE, &bar[0]);
-    }
 
     // V. Row-inverse operand: tile = parity of the block column, row (y, slot).
     {
@@ -774,6 +773,12 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_sweep_tc(const __grid_constan
     }
     phase ^= 1;
     tc::fence_after_sync();
+    // A1 (the operand tile's space) is consumed: the next row's tile starts
+    // moving in while the overlap-add runs.
+    if (tid == 0 && m + 1 < M1) {
+      tc::mbar_expect_tx(&bar[0], S::TILE);
+      tc::bulk_load(sm + S::A2, tile_of(m + 1), S::TILE, &bar[0]);
+    }
 
     // O. Overlap-add. Thread: block row y of block bl; y < n/2 finishes cell
     // row m-1 (P_old), y >= n/2 starts cell row m (P_new).

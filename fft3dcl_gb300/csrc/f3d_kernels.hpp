@@ -191,7 +191,7 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
 // Tensor-core sweep: cells per strip, CTAs per SM, and the launches (filter,
 // inverse + overlap-add, seam merge of f3d_k_sweep.cu).
 constexpr int kTcSweepCells = 7;
-constexpr int kTcSweepCtasPerSm = 2;
+constexpr int kTcSweepCtasPerSm = 3;
 cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark);
 // Bytes of SweepArgs::img for this geometry and strip count.
 size_t tc_image_bytes(const Geo& g, int strips);
