@@ -172,7 +172,14 @@ __device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
 __device__ __forceinline__ void split_pair(float a, float b, uint32_t& hi, uint32_t& lo) {
   const __half2 h = __floats2half2_rn(a, b);
   const float2 hf = __half22float2(h);
+#if __CUDA_ARCH__ >= 1000
+  // Both residuals in one packed op: hf * -1 + (a, b), rounded once per lane
+  // like the scalar subtraction.
+  const float2 r = __ffma2_rn(hf, make_float2(-1.0f, -1.0f), make_float2(a, b));
+  const __half2 l = __floats2half2_rn(r.x, r.y);
+#else
   const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+#endif
   hi = *reinterpret_cast<const uint32_t*>(&h);
   lo = *reinterpret_cast<const uint32_t*>(&l);
 }
