@@ -44,6 +44,12 @@ WORKLOAD = ("3840x2160 YUV420P10 luma, sigma=3 bt=4 bw=bh=32 ow=oh=16 sharpen=0.
 # kernel from one ncu capture of this workload (launch list of
 # `bench.py --steps 2 --warmup 3`), keyed by form; None until captured.
 NCU_TRAFFIC = {"tc": 571806464 + 130638592}
+# The same for the filter launch of a batch step of k consecutive outputs
+# (k -> bytes): captured on the 1920x1080 case of this workload (`--size
+# 1920x1080 --steps 1 --warmup 3 --no-cpu --serve-streams 0 --no-yuv
+# --compare tc`, mean of the 4-output launches: 260.2 MB read + 124.4 MB
+# written) and scaled to 3840x2160 by the block count (32912 / 8540).
+NCU_TRAFFIC_BATCH = {4: 1002927925 + 479516689}
 
 
 def algorithmic_bytes(nb: int, fbw: int, bh: int, bt: int) -> dict:
@@ -336,15 +342,18 @@ def run_gpu(args, rank, world, local_rank):
             eng.process_device(win, out.data_ptr(), pitch)
             eng.prune(n - cur - 1, n - cur + bt)
 
-        def step_batch(n):
+        def step_batch(n, b=None, ahead_in_step=True):
+            b = batch if b is None else b
             wins = [[m - cur + i for i in range(bt)] for m in range(n, n + k)]
             for w in wins:
                 for fn in w:
                     if not eng.has(fn):
                         eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
-            ahead = [n + k - 1 - cur + bt + i for i in range(k)]  # the frames after the last window
-            batch.step(ahead, [clip_dev[a % nfr].data_ptr() for a in ahead], [pitch] * k, wins,
-                       [o.data_ptr() for o in outs[:k]], [pitch] * k)
+            # The frames after the last window, forwarded concurrently with the
+            # outputs (or, for kernel timing, by the next step's engine calls).
+            ahead = [n + k - 1 - cur + bt + i for i in range(k)] if ahead_in_step else [-1] * k
+            b.step(ahead, [clip_dev[a % nfr].data_ptr() for a in ahead], [pitch] * k, wins,
+                   [o.data_ptr() for o in outs[:k]], [pitch] * k)
             eng.prune(n - cur - 1, n + k - 1 - cur + bt + k)
 
         step = step_batch if batched else step_engine
@@ -381,8 +390,25 @@ def run_gpu(args, rank, world, local_rank):
             kt += np.array(eng.last_kernel_ms())
         kt /= args.steps
         if batch is not None:
-            forms_extra["tune"] = batch.tune()
+            tune = batch.tune()
+            forms_extra["tune"] = tune
             batch.close()
+            # The batch step's own filter and inverse launches (k outputs per
+            # launch), same launch shape, without a graph so that events
+            # bracket them, and with the forwards outside the step so that no
+            # concurrent kernel shares the GPU while they run.
+            tb = F.Batch([eng] * k, graph=False, autotune=False)
+            tb.set_tune(tune["fwd_ctas_per_sm"], tune["filter_minb"])
+            bkt = np.zeros(2)
+            for _ in range(max(3, args.warmup)):
+                step_batch(n, tb, ahead_in_step=False)
+                n += k
+            for _ in range(args.steps):
+                step_batch(n, tb, ahead_in_step=False)
+                n += k
+                bkt += np.array(tb.last_kernel_ms())
+            tb.close()
+            forms_extra["batch_kernel_ms"] = [float(x) for x in bkt / args.steps]
         return ms, kt, launches, clk, eng, stream, n, k
 
     # Other forms first (device throughput only), then the headline form.
@@ -519,6 +545,22 @@ def run_gpu(args, rank, world, local_rank):
         kname, kbytes = "k_inverse (filter+inverse)", ab["filter_inverse"]
         kt_names = ("forward", "filter_inverse", "overlap_add")
     achieved = kbytes / (inv_ms / 1000.0) / 1e9 if inv_ms > 0 else None
+    roof_single = {"kernel": kname, "bound": "hbm",
+                   "achieved": achieved and round(achieved, 1), "peak": peak, "unit": "GB/s",
+                   "frac": achieved and round(achieved / peak, 4),
+                   "traffic": NCU_TRAFFIC.get(args.form), "algorithmic_bytes": kbytes,
+                   "peak_source": f"{peak_kind} hbm_gbs"}
+    roof = roof_single
+    bkt = forms_extra.get("batch_kernel_ms")
+    if bkt and kframes > 1 and info.form == 2 and info.fused:
+        # The headline step's own filter launch: kframes consecutive outputs,
+        # each reading its bt window spectra (shared ones from L2).
+        bbytes = kframes * kbytes
+        bach = bbytes / (bkt[0] / 1000.0) / 1e9
+        roof = {"kernel": f"k_filter_tc, {kframes} consecutive outputs per launch (the headline batch step)",
+                "bound": "hbm", "achieved": round(bach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(bach / peak, 4), "traffic": NCU_TRAFFIC_BATCH.get(kframes),
+                "algorithmic_bytes": bbytes, "peak_source": f"{peak_kind} hbm_gbs"}
     line = {
         "metric": METRIC, "value": round(fps, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
@@ -530,12 +572,11 @@ def run_gpu(args, rank, world, local_rank):
                    "inputs": f"clip resident in HBM ({len(frames)} x 16.6 MB)",
                    "l2": "working set per step ~750 MB: four 143 MB window spectra, larger than the 129 MB L2"},
         "kernel_ms": {kt_names[i]: round(float(kt[i]), 4) for i in range(3)},
+        "batch_kernel_ms": bkt and {"filter": round(bkt[0], 4), "inverse_overlap_add_merge": round(bkt[1], 4),
+                                    "outputs_per_launch": kframes},
         "forms": forms,
-        "roofline": {"kernel": kname, "bound": "hbm",
-                     "achieved": achieved and round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": achieved and round(achieved / peak, 4),
-                     "traffic": NCU_TRAFFIC.get(args.form), "algorithmic_bytes": kbytes,
-                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "roofline": roof,
+        "roofline_single_output": roof_single,
         "roofline_step": {"algorithmic_bytes": ab["frame"],
                           "achieved": round(ab["frame"] * fps / world / 1e9, 1), "unit": "GB/s",
                           "frac": round(ab["frame"] * fps / world / 1e9 / peak, 4)},

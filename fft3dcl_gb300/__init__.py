@@ -101,7 +101,7 @@ EXPORTS = (
     "f3d_server_create", "f3d_server_destroy", "f3d_server_open", "f3d_server_submit", "f3d_server_poll",
     "f3d_server_close", "f3d_server_get_stats",
     "f3d_batch_create", "f3d_batch_destroy", "f3d_batch_error", "f3d_batch_step", "f3d_batch_tune",
-    "f3d_batch_set_tune",
+    "f3d_batch_set_tune", "f3d_batch_last_kernel_ms",
 )
 
 _lib = None
@@ -148,6 +148,7 @@ def lib():
         L.f3d_batch_step.argtypes = [vp, P(i), P(vp), P(sz), P(P(i)), P(i), P(vp), P(sz)]
         L.f3d_batch_tune.argtypes = [vp, P(i), P(i)]
         L.f3d_batch_set_tune.argtypes = [vp, i, i]
+        L.f3d_batch_last_kernel_ms.argtypes = [vp, P(C.c_float)]
         L.f3d_server_create.argtypes = [P(ServerConfig), P(vp)]
         L.f3d_server_destroy.argtypes = [vp]
         L.f3d_server_destroy.restype = None
@@ -615,6 +616,14 @@ class Batch:
         a, b = C.c_int(), C.c_int()
         tuned = lib().f3d_batch_tune(self._h, C.byref(a), C.byref(b))
         return {"tuned": bool(tuned), "fwd_ctas_per_sm": a.value, "filter_minb": b.value}
+
+    def last_kernel_ms(self) -> list[float]:
+        """[filter, inverse + overlap-add + seam merge] device ms of the last
+        step with outputs that ran outside a CUDA graph."""
+        ms = (C.c_float * 2)()
+        if lib().f3d_batch_last_kernel_ms(self._h, ms) != F3D_OK:
+            raise F3DError(lib().f3d_batch_error(self._h).decode())
+        return [ms[0], ms[1]]
 
     def set_tune(self, fwd_ctas_per_sm: int, filter_minb: int):
         """Pins the launch shape (every shape gives the same results)."""

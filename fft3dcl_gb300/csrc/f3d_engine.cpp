@@ -787,6 +787,10 @@ struct f3d_batch {
   // Side stream of the forward when it does not feed this step's outputs.
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  // Kernel timing of the last step run outside a graph: before the filter,
+  // after it, after the inverse kernels.
+  cudaEvent_t kev[3] = {nullptr, nullptr, nullptr};
+  bool ktimed = false;
   // Entries whose engine appeared earlier in the batch (one more output of
   // that plane per step) have operand tiles and seam rows of their own.
   std::vector<uint8_t*> img;   // per entry, null: the engine's own
@@ -866,7 +870,9 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
   }
   if (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&b->kev[0]) != cudaSuccess || cudaEventCreate(&b->kev[1]) != cudaSuccess ||
+      cudaEventCreate(&b->kev[2]) != cudaSuccess) {
     cudaGetLastError();
     f3d_batch_destroy(b);
     return fail_thread(F3D_E_CUDA, "FFT3DCL: batch stream creation failed");
@@ -892,6 +898,8 @@ void f3d_batch_destroy(f3d_batch* b) {
   }
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
+  for (cudaEvent_t ev : b->kev)
+    if (ev) cudaEventDestroy(ev);
   if (b->side) cudaStreamDestroy(b->side);
   for (uint8_t* p : b->img)
     if (p) cudaFree(p);
@@ -960,6 +968,19 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
           for (int k = 0; k < nwin[j]; k++)
             if (windows[j][k] == fns[i]) overlap = false;
   if (overlap) mask |= 1u << 16;
+  // Filter, inverse and seam merge; timed by events unless being captured.
+  auto sweep = [&](const TcTune& t) -> cudaError_t {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(b->stream, &cs);
+    const bool timed = cs == cudaStreamCaptureStatusNone;
+    if (timed) cudaEventRecord(b->kev[0], b->stream);
+    cudaError_t ce = launch_sweep_tc_batch(sa, ns, t, b->stream, timed ? b->kev[1] : nullptr);
+    if (timed && ce == cudaSuccess) {
+      cudaEventRecord(b->kev[2], b->stream);
+      b->ktimed = true;
+    }
+    return ce;
+  };
   auto launch = [&](const TcTune& t) -> cudaError_t {
     cudaError_t ce = cudaSuccess;
     if (overlap) {
@@ -967,12 +988,12 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
       if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
       if (ce == cudaSuccess) ce = launch_forward_tc_batch(fa, nf, t, b->side);
       if (ce == cudaSuccess) ce = cudaEventRecord(b->join, b->side);
-      if (ce == cudaSuccess) ce = launch_sweep_tc_batch(sa, ns, t, b->stream, nullptr);
+      if (ce == cudaSuccess) ce = sweep(t);
       if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->stream, b->join, 0);
       return ce;
     }
     ce = nf ? launch_forward_tc_batch(fa, nf, t, b->stream) : cudaSuccess;
-    if (ce == cudaSuccess && ns) ce = launch_sweep_tc_batch(sa, ns, t, b->stream, nullptr);
+    if (ce == cudaSuccess && ns) ce = sweep(t);
     return ce;
   };
   // Autotuner: on the first step in which every plane enters a new frame,
@@ -1052,6 +1073,18 @@ int f3d_batch_tune(f3d_batch* b, int* fwd_ctas_per_sm, int* filter_minb) {
   if (fwd_ctas_per_sm) *fwd_ctas_per_sm = b->tune.fwd_ctas_per_sm;
   if (filter_minb) *filter_minb = b->tune.filter_minb;
   return b->tuned ? 1 : 0;
+}
+
+int f3d_batch_last_kernel_ms(f3d_batch* b, float* ms) {
+  if (!b || !ms) return fail_thread(F3D_E_PARAM, "FFT3DCL: null argument");
+  if (!b->ktimed) return batch_fail(b, F3D_E_STATE, "FFT3DCL: no batch step with outputs ran outside a CUDA graph");
+  cudaSetDevice(b->eng[0]->device);
+  cudaError_t ce = cudaEventSynchronize(b->kev[2]);
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms[0], b->kev[0], b->kev[1]);
+  if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms[1], b->kev[1], b->kev[2]);
+  if (ce != cudaSuccess)
+    return batch_fail(b, F3D_E_CUDA, std::string("FFT3DCL: batch kernel timing: ") + cudaGetErrorString(ce));
+  return F3D_OK;
 }
 
 int f3d_batch_set_tune(f3d_batch* b, int fwd_ctas_per_sm, int filter_minb) {

@@ -280,6 +280,11 @@ int f3d_batch_tune(f3d_batch* b, int* fwd_ctas_per_sm, int* filter_minb);
  * 2, filter_minb 3..5 filter CTAs per SM. Every shape gives the same
  * results. F3D_E_PARAM for any other shape. */
 int f3d_batch_set_tune(f3d_batch* b, int fwd_ctas_per_sm, int filter_minb);
+/* Device times (ms) of the last step with outputs that ran outside a CUDA
+ * graph (steps replayed as a graph are not timed): ms[0] the filter kernel,
+ * ms[1] the inverse + overlap-add kernel and the seam merge. Waits for that
+ * step. F3D_E_STATE when no such step ran. */
+int f3d_batch_last_kernel_ms(f3d_batch* b, float* ms);
 
 /* ---- Serving loop ----------------------------------------------------------
  * Replaces the reference's one-instance-per-clip model (src/fft3dcl.cpp:289,

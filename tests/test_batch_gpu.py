@@ -113,6 +113,28 @@ def test_every_launch_shape_equals_engines(bt):
                 np.testing.assert_array_equal(g, r, err_msg=f"shape {shape} plane {i} frame {n}")
 
 
+def test_batch_kernel_times():
+    import torch
+    frames = synth.moving_rects(320, 192, 6, 61, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.Stream(device=dev)
+    src = torch.from_numpy(np.stack(frames)).to(dev)
+    dst = torch.empty((192, 320), dtype=torch.uint16, device=dev)
+    with F.Engine(320, 192, 10, form="tc", stream=st.cuda_stream, bt=3) as e:
+        b = F.Batch([e], graph=False, autotune=False)
+        try:
+            with pytest.raises(F.F3DError):
+                b.last_kernel_ms()  # no step yet
+            with torch.cuda.stream(st):
+                for fn in range(3):
+                    e.forward_device(fn, src[fn].data_ptr(), 640)
+                b.step([-1], [src[0].data_ptr()], [640], [[0, 1, 2]], [dst.data_ptr()], [640])
+            ms = b.last_kernel_ms()
+            assert len(ms) == 2 and all(0.0 < t < 1000.0 for t in ms)
+        finally:
+            b.close()
+
+
 def test_set_tune_rejects_unknown_shapes():
     eng = F.Engine(128, 96, 8, form="tc", bt=3)
     b = F.Batch([eng])
