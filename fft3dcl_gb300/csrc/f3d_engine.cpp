@@ -1001,7 +1001,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   // all of them; the last run leaves it in place) and keep the fastest.
   const unsigned all = (1u << n) - 1;
   if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFu) == (all | (all << 8))) {
-    const TcTune cands[] = {{2, 5}, {1, 5}, {2, 4}, {1, 4}, {2, 3}, {1, 3}};
+    const TcTune cands[] = {{3, 5}, {2, 5}, {1, 5}, {3, 4}, {2, 4}, {1, 4}, {3, 3}, {2, 3}, {1, 3}};
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
@@ -1089,7 +1089,7 @@ int f3d_batch_last_kernel_ms(f3d_batch* b, float* ms) {
 
 int f3d_batch_set_tune(f3d_batch* b, int fwd_ctas_per_sm, int filter_minb) {
   if (!b) return fail_thread(F3D_E_PARAM, "FFT3DCL: null batch");
-  if (fwd_ctas_per_sm < 1 || fwd_ctas_per_sm > 2 || filter_minb < 3 || filter_minb > 5)
+  if (fwd_ctas_per_sm < 1 || fwd_ctas_per_sm > 3 || filter_minb < 3 || filter_minb > 5)
     return batch_fail(b, F3D_E_PARAM, "FFT3DCL: unsupported launch shape");
   cudaSetDevice(b->eng[0]->device);
   if (b->stream) cudaStreamSynchronize(b->stream);

@@ -87,25 +87,29 @@ constexpr uint64_t kWaitNs = 1000000000ull;  // one second
 // ---- forward ---------------------------------------------------------------
 
 // Shared memory of the forward kernel (offsets from a 1024-aligned base).
-// A1, A2 and the staging area of the spectra are live at the same time: the
-// next group's step-1 operand is deposited while step 2 of the current group
-// runs, and a group's bulk store drains while the next group is transformed.
-// Without the split (integer samples of up to 11 bits) A1 holds only the hi
-// parts, and two CTAs fit on an SM.
+// A1 and A2 are live at the same time (the next group's step-1 operand is
+// deposited while step 2 of the current group runs). The staging area of a
+// group's spectra shares A2's space: it is written once step 2 has read A2,
+// and its bulk store has drained before the next group writes A2. Without the
+// split (integer samples of up to 11 bits) A1 holds only the hi parts: 73 KB,
+// three CTAs per SM; with the split 88 KB, two.
 template <int N, bool SPLIT>
 struct FwdSmem {
   using C = TcCfg<N>;
   static constexpr uint32_t A1_TILE = (SPLIT ? 2 : 1) * C::A1_BYTES;  // hi[, lo] of one step-1 tile
+  static constexpr uint32_t STAGE_BYTES = C::G * C::PS * 8;           // float2 [G][N][FBW]
   static constexpr uint32_t B2 = 0;                       // hi, lo
   static constexpr uint32_t B1 = B2 + 2 * C::B2_BYTES;    // hi, lo
   static constexpr uint32_t A2 = (B1 + 2 * C::B1_BYTES + 1023) / 1024 * 1024;  // hi, lo (SWIZZLE_128B)
-  static constexpr uint32_t A1 = A2 + 2 * C::A2_BYTES;    // [tile][hi, lo]
-  static constexpr uint32_t STAGE = A1 + C::T1 * A1_TILE; // float2 [G][N][FBW]
-  static constexpr uint32_t BAR = STAGE + C::G * C::PS * 8;
+  static constexpr uint32_t STAGE = A2;
+  static constexpr uint32_t A1 = A2 + (2 * C::A2_BYTES > STAGE_BYTES ? 2 * C::A2_BYTES : STAGE_BYTES);
+  static constexpr uint32_t BAR = A1 + C::T1 * A1_TILE;   // [tile][hi, lo]
   static constexpr uint32_t TSLOT = BAR + 16;
   static constexpr uint32_t BYTES = TSLOT + 16 + 1024;    // + alignment slack
-  static_assert(STAGE % 16 == 0 && BAR % 16 == 0, "bulk-copy source alignment");
+  static_assert(STAGE % 16 == 0 && A1 % 128 == 0 && BAR % 16 == 0, "bulk-copy and operand alignment");
 };
+// CTAs per SM of the forward kernel: the launch bound, and what fits.
+constexpr int kFwdMaxCtasPerSm = 3;
 
 // Gather of a group's samples: task q covers 16 source bytes (16/BPS samples)
 // of row y of block bl. The raw bytes are fetched into registers one group
@@ -206,7 +210,7 @@ __device__ __forceinline__ int plane_of(const Batch& b, const int (&prefix)[kMax
 }
 
 template <int N, int BPS, bool SPLIT>
-__global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_constant__ TcFwdBatch B) {
+__global__ void __launch_bounds__(kTcThreads, kFwdMaxCtasPerSm) k_forward_tc(const __grid_constant__ TcFwdBatch B) {
   using C = TcCfg<N>;
   using L = FwdSmem<N, SPLIT>;
   using T = TcTab<N>;
@@ -296,8 +300,10 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     const TcFwdArgs& a = B.p[pl];
     const int b0 = (grp - B.grp0[pl]) * C::G;
     const int nvalid = min(C::G, a.g.nb - b0);
-    // Every thread takes the same branch: a wait that gave up anywhere ends
-    // the sweep of groups for the whole CTA.
+    // The previous group's bulk store must have read the staging area, which
+    // shares A2's space (written next). Every thread takes the same branch: a
+    // wait that gave up anywhere ends the sweep of groups for the whole CTA.
+    if (tid == 0) tc::bulk_wait_read();
     if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
       if (tid == 0) atomicOr(a.err, 1);
       break;
@@ -345,8 +351,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_forward_tc(const __grid_const
     // 5. The next group's operand and step 1 (every warp has read D1 above).
     if (grp + (int)gridDim.x < ngroups) begin_group(grp + gridDim.x);
 
-    // The previous group's bulk store must have read the staging area.
-    if (tid == 0) tc::bulk_wait_read();
+    // Step 2 done: A2's space is free for the staging area.
     if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
       if (tid == 0) atomicOr(a.err, 1);
       break;
@@ -1025,7 +1030,7 @@ cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune
   TcFwdBatch B;
   if (!forward_batch(planes, n, B)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
   // The split kernel (hi + lo step-1 operand) also takes planes that need no
-  // split; it fits one CTA per SM, the other two.
+  // split; it fits two CTAs per SM, the other three.
   bool split = false;
   for (int i = 0; i < n; i++) split = split || planes[i].split;
   const int fmt = planes[0].fmt;
@@ -1038,7 +1043,9 @@ cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune
   if (attr != cudaSuccess) return attr;
   const int ngroups = B.grp0[n];
   if (ngroups == 0) return cudaSuccess;
-  const int per_sm = split ? 1 : std::max(1, std::min(t.fwd_ctas_per_sm, 2));
+  const int per_sm = std::max(1, std::min(t.fwd_ctas_per_sm, split ? 2 : kFwdMaxCtasPerSm));
+  static_assert(kFwdMaxCtasPerSm * (FwdSmem<32, false>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
+  static_assert(2 * (FwdSmem<32, true>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
   const int grid = std::min(ngroups, per_sm * sm_count());
   k<<<grid, kTcThreads, smem, st>>>(B);
   count_launch();

@@ -276,8 +276,8 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
                    const int* const* windows, const int* nwin, void* const* dev_dst, const size_t* dst_pitch);
 /* Launch shape in use; returns 1 when the autotuner has chosen it. */
 int f3d_batch_tune(f3d_batch* b, int* fwd_ctas_per_sm, int* filter_minb);
-/* Pins the launch shape (the autotuner then keeps it): fwd_ctas_per_sm 1 or
- * 2, filter_minb 3..5 filter CTAs per SM. Every shape gives the same
+/* Pins the launch shape (the autotuner then keeps it): fwd_ctas_per_sm 1 to
+ * 3 forward CTAs per SM, filter_minb 3..5 filter CTAs per SM. Every shape gives the same
  * results. F3D_E_PARAM for any other shape. */
 int f3d_batch_set_tune(f3d_batch* b, int fwd_ctas_per_sm, int filter_minb);
 /* Device times (ms) of the last step with outputs that ran outside a CUDA

@@ -95,17 +95,17 @@ def test_yuv_planes_batch_equals_engines(flags):
         for n, (g, r) in enumerate(zip(got[i], ref[i])):
             np.testing.assert_array_equal(g, r, err_msg=f"plane {i} frame {n}")
     if flags & 2:
-        assert tune["tuned"] and tune["fwd_ctas_per_sm"] in (1, 2) and tune["filter_minb"] in (3, 4, 5)
+        assert tune["tuned"] and tune["fwd_ctas_per_sm"] in (1, 2, 3) and tune["filter_minb"] in (3, 4, 5)
 
 
 @pytest.mark.parametrize("bt", [-1, 1, 2, 3, 4])
 def test_every_launch_shape_equals_engines(bt):
-    # Every filter-kernel variant (5, 4, 3 CTAs per SM) and forward grid (1,
-    # 2 CTAs per SM): the same bits as the engines, in every temporal mode.
+    # Every filter-kernel variant (5, 4, 3 CTAs per SM) and forward grid (1
+    # to 3 CTAs per SM): the same bits as the engines, in every temporal mode.
     planes = yuv420(400, 240, 6, 31 + bt, 10)[:2]
     params = dict(sigma=3.0, bt=bt, sharpen=0.3, degrid=1.0)
     ref, _ = run_planes(planes, params, [False, True], 10, None)
-    for shape in [(2, 5), (1, 5), (2, 4), (1, 3)]:
+    for shape in [(3, 5), (2, 5), (1, 5), (2, 4), (3, 3)]:
         got, tune = run_planes(planes, params, [False, True], 10, 1, shape=shape)
         assert (tune["fwd_ctas_per_sm"], tune["filter_minb"]) == shape
         for i in range(2):
@@ -139,7 +139,7 @@ def test_set_tune_rejects_unknown_shapes():
     eng = F.Engine(128, 96, 8, form="tc", bt=3)
     b = F.Batch([eng])
     try:
-        for shape in [(3, 5), (0, 5), (2, 2), (2, 6)]:
+        for shape in [(4, 5), (0, 5), (2, 2), (2, 6)]:
             with pytest.raises(F.F3DError):
                 b.set_tune(*shape)
         b.set_tune(1, 3)
