@@ -564,9 +564,12 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
 
   const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
   // The group's window spectra start moving into L2 as whole runs, so that
-  // the bins' loads below mostly wait on L2 rather than on DRAM.
+  // the bins' loads below mostly wait on L2 rather than on DRAM. Of shifted
+  // windows (consecutive outputs, their CTAs side by side), each later output
+  // pulls only its newest frame: the others are an earlier output's.
   constexpr uint32_t BIN_BYTES = HALF ? 4 : 8;
-  if (F3D_TC_FILTER_PREFETCH && tid < NF && nvbin > 0)
+  const bool pull = !B.shifted || pl == 0 || tid == NF - 1;
+  if (F3D_TC_FILTER_PREFETCH && tid < NF && nvbin > 0 && pull)
     tc::prefetch_l2(reinterpret_cast<const uint8_t*>(a.s[tid]) + gb0 * BIN_BYTES, (uint32_t)(nvbin * BIN_BYTES));
   if (tid < C::G) {
     const int n = J0 + tid;
@@ -1021,6 +1024,13 @@ bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& B
   for (int i = 1; i < n; i++)
     if (B.p[i].inv.g.W != B.p[0].inv.g.W || B.p[i].inv.g.H != B.p[0].inv.g.H || B.p[i].strips != B.p[0].strips)
       Bf.interleave = 0;
+  // Consecutive outputs of one plane: every window frame but the newest is
+  // the previous entry's (the same spectrum buffers).
+  const int nf = B.p[0].inv.bm >= 2 ? B.p[0].inv.bm : 1;
+  Bf.shifted = Bf.interleave && n > 1 && nf > 1;
+  for (int i = 1; i < n && Bf.shifted; i++)
+    for (int k = 0; k + 1 < nf; k++)
+      if (B.p[i].inv.s[k] != B.p[i - 1].inv.s[k + 1]) Bf.shifted = 0;
   prefix(Bs, [](const SweepArgs& a) { return a.strips * a.segs; });          // (strip, segment)
   prefix(Bm, [](const SweepArgs& a) { return a.segs > 1 ? a.segs - 1 : 0; });  // seams
   return true;

@@ -173,6 +173,7 @@ struct SweepBatch {
   int n;
   int cta0[kMaxBatch + 1];
   int interleave;  // filter: planes of one geometry, CTA i is group i / n of plane i % n
+  int shifted;     // filter, interleaved: plane i's window is plane i-1's shifted by one frame
   SweepArgs p[kMaxBatch];
 };
 // Launch shape of the tensor-core kernels, picked by the autotuner.
