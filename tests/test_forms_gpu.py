@@ -124,6 +124,8 @@ def test_form_golden_within_tolerance(form, path):
     (1000, 37, dict(bt=-1, sharpen=0.3)),
     (41, 700, dict(bt=4, sigma2=1.0, sigma3=3.0, sigma4=4.0)),
     (1920, 1080, dict(bt=1, degrid=0.0)),
+    (24, 20, dict(bt=3)),
+    (16, 16, dict(bt=4, sharpen=0.4)),
 ])
 def test_tc_sweep_sizes(w, h, params):
     # The tensor-core sweep on planes with ragged edges, one and many
@@ -136,3 +138,25 @@ def test_tc_sweep_sizes(w, h, params):
     flt.close()
     ref = oracle.run_clip(frames, 8, threads=16, **params)
     check(got, ref, 1)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("bits", [8, 10])
+def test_form_yuv_planes_within_tolerance(form, bits):
+    # All three planes of a YUV 4:2:0 clip: the chroma planes take the mode-1
+    # chroma offset (src/cpu/reference.cpp:72-79; in the tensor-core form, the
+    # window spectrum's correction), each plane against the oracle.
+    w, h, n = 352, 208, 6
+    maxval = (1 << bits) - 1
+    kw = {} if bits == 8 else dict(dtype=np.uint16, maxval=maxval)
+    s = 1 if bits == 8 else 4
+    y = synth.moving_rects(w, h, n, 91 + bits, lo=16 * s, hi=235 * s, noise=2.5 * s, **kw)
+    u = synth.moving_rects(w // 2, h // 2, n, 92 + bits, lo=16 * s, hi=240 * s, noise=1.5 * s, ramp=False, **kw)
+    v = synth.moving_rects(w // 2, h // 2, n, 93 + bits, lo=16 * s, hi=240 * s, noise=1.5 * s, ramp=False, **kw)
+    params = dict(sigma=2.5, bt=4, sharpen=0.4, plane=4)
+    clip = [[y[i], u[i], v[i]] for i in range(n)]
+    got = F.FFT3DCL(clip, F.VideoFormat("yuv", bits, 0, 1, 1), form=form, **params)
+    tol = 1 if bits == 8 else 4
+    for p, plane in enumerate([y, u, v]):
+        ref = oracle.run_clip([plane[i] for i in range(n)], bits, threads=16, chroma=p > 0, **params)
+        check([g[p] for g in got], ref, tol)
