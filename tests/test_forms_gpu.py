@@ -49,6 +49,8 @@ CASES = [
     ("float_bt3", lambda: synth.clip_grays(frames=5), 32, dict(bt=3, sharpen=0.3)),
     ("p12_bt2", lambda: synth.moving_rects(160, 96, 4, 7, lo=256, hi=3800, noise=20.0, dtype=np.uint16,
                                            maxval=4095), 12, dict(bt=2)),
+    ("p16_bt3_sharpen", lambda: synth.moving_rects(224, 128, 5, 8, lo=4096, hi=60000, noise=300.0, dtype=np.uint16,
+                                                   maxval=65535), 16, dict(bt=3, sharpen=0.3)),
     ("float_kalman_bw64", lambda: synth.clip_grays(frames=24, cuts=(12,)), 32,
      dict(bt=0, bw=64, bh=64, sigma2=1.5, sigma3=2.5, sigma4=3.0)),
 ]
@@ -141,22 +143,27 @@ def test_tc_sweep_sizes(w, h, params):
 
 
 @pytest.mark.parametrize("form", FORMS)
-@pytest.mark.parametrize("bits", [8, 10])
+@pytest.mark.parametrize("bits", [8, 10, 32])
 def test_form_yuv_planes_within_tolerance(form, bits):
     # All three planes of a YUV 4:2:0 clip: the chroma planes take the mode-1
     # chroma offset (src/cpu/reference.cpp:72-79; in the tensor-core form, the
-    # window spectrum's correction), each plane against the oracle.
+    # window spectrum's correction), each plane against the oracle. bits=32:
+    # float samples.
     w, h, n = 352, 208, 6
-    maxval = (1 << bits) - 1
-    kw = {} if bits == 8 else dict(dtype=np.uint16, maxval=maxval)
-    s = 1 if bits == 8 else 4
+    if bits == 32:
+        kw, s = dict(dtype=np.float32, maxval=1.0), 1.0 / 255.0
+    elif bits == 8:
+        kw, s = {}, 1
+    else:
+        kw, s = dict(dtype=np.uint16, maxval=(1 << bits) - 1), 4
     y = synth.moving_rects(w, h, n, 91 + bits, lo=16 * s, hi=235 * s, noise=2.5 * s, **kw)
     u = synth.moving_rects(w // 2, h // 2, n, 92 + bits, lo=16 * s, hi=240 * s, noise=1.5 * s, ramp=False, **kw)
     v = synth.moving_rects(w // 2, h // 2, n, 93 + bits, lo=16 * s, hi=240 * s, noise=1.5 * s, ramp=False, **kw)
     params = dict(sigma=2.5, bt=4, sharpen=0.4, plane=4)
     clip = [[y[i], u[i], v[i]] for i in range(n)]
-    got = F.FFT3DCL(clip, F.VideoFormat("yuv", bits, 0, 1, 1), form=form, **params)
-    tol = 1 if bits == 8 else 4
+    fmt = F.VideoFormat("yuv", bits, 1 if bits == 32 else 0, 1, 1)
+    got = F.FFT3DCL(clip, fmt, form=form, **params)
+    tol = 1e-4 if bits == 32 else (1 if bits == 8 else 4)
     for p, plane in enumerate([y, u, v]):
         ref = oracle.run_clip([plane[i] for i in range(n)], bits, threads=16, chroma=p > 0, **params)
         check([g[p] for g in got], ref, tol)
