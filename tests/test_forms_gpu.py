@@ -43,6 +43,12 @@ CASES = [
      dict(bt=1, sigma2=1.0, sigma3=3.0, sigma4=4.0)),
     ("gray8_btm1", lambda: synth.clip_gray8(frames=2), 8, dict(bt=-1, sharpen=0.7)),
     ("gray8_bw16_wintype1", lambda: synth.clip_gray8(frames=5), 8, dict(bw=16, bh=16, wintype=1)),
+    # 32x32 blocks: the tensor-core form folds these windows into its DFT matrices.
+    ("gray8_wintype1", lambda: synth.clip_gray8(frames=5), 8, dict(bt=3, wintype=1, sharpen=0.3)),
+    ("gray8_wintype2", lambda: synth.clip_gray8(frames=5), 8, dict(bt=4, wintype=2)),
+    ("p10_wintype2", lambda: synth.moving_rects(320, 176, 5, 11, lo=64, hi=960, noise=8.0,
+                                                            dtype=np.uint16, maxval=1023), 10,
+     dict(bt=2, wintype=2, sharpen=0.2)),
     ("gray8_bw8x64_overlap", lambda: synth.clip_gray8(frames=5), 8, dict(bw=8, bh=64, ow=2, oh=16)),
     ("gray8_mode0", lambda: synth.clip_gray8(frames=5), 8, dict(mode=0, bw=16, bh=32)),
     ("p10_4k_bt4", lambda: synth.clip_yuv420p10_luma(frames=5), 10, dict(sigma=3.0, bt=4, sharpen=0.4)),
