@@ -532,6 +532,51 @@ __device__ __forceinline__ float2 spec_at(const float2* s, size_t j) {
   else return s[j];
 }
 
+// R. Row (k', block), K = 2 ky + (re, im) of the operand image of group
+// (m, strip) from its filtered bins fbuf[block][bin], in 16-byte chunks of 4
+// ky. Block 0 also goes to the previous strip's tile as its block 7; this
+// tile's block 7 comes from the next strip.
+template <int N>
+__device__ __forceinline__ void operand_tile(const SweepArgs& sa, int m, int strip, const float2* fbuf, int tid) {
+  using C = TcCfg<N>;
+  using S = SwpCfg<N>;
+  const bool last_strip = strip == sa.strips - 1;
+  uint8_t* img = sa.img + ((size_t)m * sa.strips + strip) * S::TILE;
+  uint8_t* prev = strip > 0 ? img - S::TILE : nullptr;
+  const int r2 = tid & 127, h = tid >> 7;
+  const int kp = r2 >> 3, bl = r2 & 7;
+  if (bl == C::G - 1 && !last_strip) return;
+  const float2* fb = fbuf + bl * S::FS;
+#pragma unroll
+  for (int cq = 0; cq < C::NY / 4; cq++) {
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int ky = C::NY * h + 4 * cq + u;
+      float2 z;
+      if (kp == 0) {
+        const int kym = (N - ky) & (N - 1);
+        const float2 f0 = fb[ky * C::FBW], f0m = fb[kym * C::FBW];
+        const float2 fn = fb[ky * C::FBW + C::NY], fnm = fb[kym * C::FBW + C::NY];
+        const float h0x = 0.5f * (f0.x + f0m.x), h0y = 0.5f * (f0.y - f0m.y);
+        const float hnx = 0.5f * (fn.x + fnm.x), hny = 0.5f * (fn.y - fnm.y);
+        z = make_float2(h0x - hny, h0y + hnx);
+      } else {
+        z = fb[ky * C::FBW + kp];
+      }
+      tc::split_pair(z.x * kInvPre, z.y * kInvPre, hi[u], lo[u]);
+    }
+    const uint32_t o = tc::off_sw128(r2, 2 * (C::NY * h + 4 * cq));
+    *reinterpret_cast<uint4*>(img + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    *reinterpret_cast<uint4*>(img + C::A2_BYTES + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    if (bl == 0 && prev) {
+      const uint32_t op = tc::off_sw128(r2 + C::G - 1, 2 * (C::NY * h + 4 * cq));
+      *reinterpret_cast<uint4*>(prev + op) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(prev + C::A2_BYTES + op) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+  }
+}
+
 template <int N, int BM, int MINB, bool HALF>
 __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_constant__ SweepBatch B) {
   using C = TcCfg<N>;
@@ -610,43 +655,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   }
   __syncthreads();
 
-  // R. Row (k', block), K = 2 ky + (re, im) of the operand image, in 16-byte
-  // chunks of 4 ky. Block 0 also goes to the previous strip's tile as its
-  // block 7; this tile's block 7 comes from the next strip.
-  uint8_t* img = sa.img + ((size_t)m * sa.strips + strip) * S::TILE;
-  uint8_t* prev = strip > 0 ? img - S::TILE : nullptr;
-  const int r2 = tid & 127, h = tid >> 7;
-  const int kp = r2 >> 3, bl = r2 & 7;
-  if (bl == C::G - 1 && !last_strip) return;
-  const float2* fb = fbuf + bl * S::FS;
-#pragma unroll
-  for (int cq = 0; cq < C::NY / 4; cq++) {
-    uint32_t hi[4], lo[4];
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const int ky = C::NY * h + 4 * cq + u;
-      float2 z;
-      if (kp == 0) {
-        const int kym = (N - ky) & (N - 1);
-        const float2 f0 = fb[ky * C::FBW], f0m = fb[kym * C::FBW];
-        const float2 fn = fb[ky * C::FBW + C::NY], fnm = fb[kym * C::FBW + C::NY];
-        const float h0x = 0.5f * (f0.x + f0m.x), h0y = 0.5f * (f0.y - f0m.y);
-        const float hnx = 0.5f * (fn.x + fnm.x), hny = 0.5f * (fn.y - fnm.y);
-        z = make_float2(h0x - hny, h0y + hnx);
-      } else {
-        z = fb[ky * C::FBW + kp];
-      }
-      tc::split_pair(z.x * kInvPre, z.y * kInvPre, hi[u], lo[u]);
-    }
-    const uint32_t o = tc::off_sw128(r2, 2 * (C::NY * h + 4 * cq));
-    *reinterpret_cast<uint4*>(img + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-    *reinterpret_cast<uint4*>(img + C::A2_BYTES + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-    if (bl == 0 && prev) {
-      const uint32_t op = tc::off_sw128(r2 + C::G - 1, 2 * (C::NY * h + 4 * cq));
-      *reinterpret_cast<uint4*>(prev + op) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-      *reinterpret_cast<uint4*>(prev + C::A2_BYTES + op) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-    }
-  }
+  operand_tile<N>(sa, m, strip, fbuf, tid);
 }
 
 template <int N>

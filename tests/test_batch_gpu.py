@@ -179,38 +179,74 @@ def test_batch_rejects_mixed_forms():
             F.Batch([e1, e2])
 
 
-@pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("k", [2, 4, 8])
-def test_several_outputs_per_step_equal_engine(k, graph):
-    # The same engine k times in a batch: k consecutive outputs per step, the
-    # forwards of the next k frames concurrent with them.
-    frames = synth.moving_rects(320, 192, 13, 51, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
-    params = dict(sigma=3.0, bt=4, sharpen=0.3)
-    ref = F.FFT3DCL(frames, bits=10, form="tc", **params)
+def consecutive_outputs(frames, bits, params, k, graph, shape=None, flags=0):
+    """The same engine k times in a batch: k consecutive outputs per step, the
+    forwards of the next k frames concurrent with them. Returns the outputs
+    and the batch's launch shape."""
+    h, w = frames[0].shape
+    ip = F.validate(w, h, bits, **params)
+    bt, cur = max(ip.bt, 1), ip.current
     dev = torch.device("cuda", 0)
     st = torch.cuda.Stream(device=dev)
-    e = F.Engine(320, 192, 10, form="tc", stream=st.cuda_stream, **params)
+    e = F.Engine(w, h, bits, form="tc", stream=st.cuda_stream, flags=flags, **params)
     src = torch.from_numpy(np.stack(frames)).to(dev)
-    dst = [torch.empty((192, 320), dtype=torch.uint16, device=dev) for _ in range(k)]
-    b = F.Batch([e] * k, graph=graph, autotune=True)
-    nfr, pitch = len(frames), 320 * 2
+    dst = [torch.empty((h, w), dtype=src.dtype, device=dev) for _ in range(k)]
+    b = F.Batch([e] * k, graph=graph, autotune=shape is None)
+    if shape is not None:
+        b.set_tune(*shape)
+    nfr, pitch = len(frames), w * frames[0].itemsize
     got = []
     with torch.cuda.stream(st):
         for n in range(0, nfr, k):
-            wins = [[min(max(m - 2 + i, 0), nfr - 1) for i in range(4)] for m in range(n, n + k)]
-            for w in wins:
-                for fn in w:
+            wins = [[min(max(m - cur + i, 0), nfr - 1) for i in range(bt)] for m in range(n, n + k)]
+            for win in wins:
+                for fn in win:
                     if not e.has(fn):
                         e.forward_device(fn, src[fn].data_ptr(), pitch)
             # The frames after the last window, unless a clamped window holds them.
-            ahead = [n + k + 1 + i for i in range(k)]
+            ahead = [n + k - 1 - cur + bt + i for i in range(k)]
             ahead = [a if a < nfr else -1 for a in ahead]
             b.step(ahead, [src[min(a, nfr - 1)].data_ptr() for a in ahead], [pitch] * k, wins,
                    [d.data_ptr() for d in dst], [pitch] * k)
             st.synchronize()
             got += [d.cpu().numpy() for d in dst]
-            e.prune(n - 3, n + 2 * k + 1)
+            e.prune(n - cur - 1, n + k - 1 - cur + bt + k)
+    tune = b.tune()
     b.close()
     e.close()
-    for n in range(nfr):
+    return got[:nfr], tune
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("k", [2, 4, 8])
+def test_several_outputs_per_step_equal_engine(k, graph):
+    frames = synth.moving_rects(320, 192, 13, 51, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
+    params = dict(sigma=3.0, bt=4, sharpen=0.3)
+    ref = F.FFT3DCL(frames, bits=10, form="tc", **params)
+    got, _ = consecutive_outputs(frames, 10, params, k, graph)
+    for n in range(len(frames)):
+        np.testing.assert_array_equal(got[n], ref[n], err_msg=f"frame {n}")
+
+
+@pytest.mark.parametrize("bits,bt,k,graph,flags,extra", [
+    (10, 4, 2, False, 0, dict(degrid=0.0)),
+    (10, 3, 4, True, 0, dict(sigma2=1.0, sigma3=3.0, sigma4=4.0)),
+    (10, 2, 6, False, 0, dict(beta=1.5, sharpen=0.5)),
+    (8, 4, 8, True, F.FLAG_HALF_SPECTRA, dict(precision=0, sharpen=0.4)),
+    (8, 2, 4, False, F.FLAG_HALF_SPECTRA, dict(precision=1)),
+])
+def test_consecutive_outputs_each_temporal_mode(bits, bt, k, graph, flags, extra):
+    # Batches of consecutive outputs (shifted windows: the filter pulls only
+    # each later output's newest frame into L2) in temporal modes 2-4, with
+    # degrid off, a sigma pattern and half storage: the per-output engine
+    # path's values bit for bit.
+    if bits == 8:
+        frames = synth.moving_rects(352, 208, 15, 61 + bt, lo=16, hi=235, noise=4.0)
+    else:
+        frames = synth.moving_rects(352, 208, 15, 61 + bt, lo=64, hi=940, noise=10.0, dtype=np.uint16,
+                                    maxval=1023)
+    params = dict(sigma=3.0, bt=bt, **extra)
+    ref = F.FFT3DCL(frames, bits=bits, form="tc", flags=flags, **params)
+    got, _ = consecutive_outputs(frames, bits, params, k, graph, flags=flags)
+    for n in range(len(frames)):
         np.testing.assert_array_equal(got[n], ref[n], err_msg=f"frame {n}")
