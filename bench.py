@@ -184,8 +184,9 @@ YUV_PARAMS = dict(sigma=2.5, bt=4, bw=32, bh=32, ow=16, oh=16, sharpen=0.4, scut
 
 def yuv_batched(args, dev, local_rank):
     """1920x1080 YUV420P8, all three planes: the tensor-core form as one
-    batch (one launch per kernel for the three planes, replayed as a CUDA
-    graph, autotuned) against the fast form's per-plane engines."""
+    batch (one launch per kernel for the three planes, or for two consecutive
+    frames' six planes, replayed as a CUDA graph, autotuned) against the fast
+    form's per-plane engines."""
     import torch
     import fft3dcl_gb300 as F
     from fft3dcl_gb300 import synth
@@ -194,57 +195,62 @@ def yuv_batched(args, dev, local_rank):
               synth.moving_rects(w // 2, h // 2, nd, 0xF3D0 + 11, lo=16, hi=240, noise=1.5, ramp=False),
               synth.moving_rects(w // 2, h // 2, nd, 0xF3D0 + 12, lo=16, hi=240, noise=1.5, ramp=False)]
     src = [torch.from_numpy(np.stack(p)).to(dev) for p in planes]
-    dst = [torch.empty(p[0].shape, dtype=torch.uint8, device=dev) for p in planes]
-    pitch = [p[0].shape[1] for p in planes]
     ip = F.validate(w, h, 8, **YUV_PARAMS)
     bt, cur = ip.bt, ip.current
     res = {}
-    for name in ("tc", "tc_half", "fast"):
-        form = "fast" if name == "fast" else "tc"
-        flags = F.FLAG_HALF_SPECTRA if name == "tc_half" else 0
+    # name: (form, storage flags, frames per step)
+    variants = {"tc": ("tc", 0, 1), "tc_2frames": ("tc", 0, 2), "tc_half": ("tc", F.FLAG_HALF_SPECTRA, 1),
+                "tc_half_2frames": ("tc", F.FLAG_HALF_SPECTRA, 2), "fast": ("fast", 0, 1)}
+    for name, (form, flags, k) in variants.items():
         st = torch.cuda.Stream(device=dev)
         engs = [F.Engine(p[0].shape[1], p[0].shape[0], 8, chroma=i > 0, form=form, device=local_rank,
                          stream=st.cuda_stream, flags=flags, **YUV_PARAMS) for i, p in enumerate(planes)]
         if flags:
             assert all(e.info().half_spectra for e in engs)
-        batch = F.Batch(engs, graph=True, autotune=True) if form == "tc" else None
+        # Batch slots by plane: [Y, U, V] for one frame, [Y, Y, U, U, V, V] for two.
+        slots = [(i, r) for i in range(3) for r in range(k)]
+        dst = [torch.empty(planes[i][0].shape, dtype=torch.uint8, device=dev) for i, _ in slots]
+        pitch = [planes[i][0].shape[1] for i, _ in slots]
+        batch = F.Batch([engs[i] for i, _ in slots], graph=True, autotune=True) if form == "tc" else None
 
         def step(n):
-            win = [n - cur + i for i in range(bt)]
-            for fn in (win if batch is not None else win[:-1]):
-                for i, e in enumerate(engs):
-                    if not e.has(fn):
-                        e.forward_device(fn, src[i][fn % nd].data_ptr(), pitch[i])
-            last = win[-1]
+            wins = [[n + r - cur + j for j in range(bt)] for _, r in slots]
+            for (i, _), win in zip(slots, wins):
+                for fn in (win if batch is not None else win[:-1]):
+                    if not engs[i].has(fn):
+                        engs[i].forward_device(fn, src[i][fn % nd].data_ptr(), pitch[i * k])
             if batch is not None:
-                # Forward one frame ahead, concurrent with this window's outputs.
-                ahead = n - cur + bt
-                batch.step([ahead] * 3, [s[ahead % nd].data_ptr() for s in src], pitch, [win] * 3,
+                # Forward the next step's entering frames, concurrent with this
+                # step's outputs.
+                ahead = [n + k - 1 - cur + bt + r for _, r in slots]
+                batch.step(ahead, [src[i][a % nd].data_ptr() for (i, _), a in zip(slots, ahead)], pitch, wins,
                            [d.data_ptr() for d in dst], pitch)
             else:
+                last = wins[0][-1]
                 for i, e in enumerate(engs):
                     if not e.has(last):
                         e.forward_device(last, src[i][last % nd].data_ptr(), pitch[i])
-                    e.process_device(win, dst[i].data_ptr(), pitch[i])
+                    e.process_device(wins[0], dst[i].data_ptr(), pitch[i])
             for e in engs:
-                e.prune(n - cur - 1, n - cur + bt)
+                e.prune(n - cur - 1, n + k - 1 - cur + bt + k)
 
         n = cur
         for _ in range(max(3, args.warmup)):
             step(n)
-            n += 1
+            n += k
         torch.cuda.synchronize(dev)
         l0 = F.kernel_launches()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        for _ in range(args.steps):
+        nsteps = max(1, args.steps // k)
+        for _ in range(nsteps):
             step(n)
-            n += 1
+            n += k
         e1.record(st)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
-        res[name] = {"frames_per_s": round(args.steps / (ms / 1000.0), 1),
-                     "launches_per_frame": round((F.kernel_launches() - l0) / args.steps, 2)}
+        res[name] = {"frames_per_s": round(nsteps * k / (ms / 1000.0), 1),
+                     "launches_per_frame": round((F.kernel_launches() - l0) / (nsteps * k), 2)}
         if batch is not None:
             res[name]["tune"] = batch.tune()
             batch.close()
@@ -252,8 +258,11 @@ def yuv_batched(args, dev, local_rank):
             e.close()
     res["tc"]["form"] = ("tensor cores, 3 planes per launch, CUDA graph per frame, forward one frame ahead "
                          "concurrent with the outputs")
+    res["tc_2frames"]["form"] = ("as tc, two consecutive frames per step: 6 planes per launch "
+                                 "([Y, Y, U, U, V, V]; each plane's two outputs share window spectra in L2)")
     res["tc_half"]["form"] = ("as tc, spectra cached as fp16 pairs (F3D_FLAG_HALF_SPECTRA: the original's "
                               "storage at precision 0, the default; opt-in, within +-1 LSB of the fp32 path)")
+    res["tc_half_2frames"]["form"] = "as tc_2frames with fp16 spectrum storage"
     res["fast"]["form"] = "fp32 radix FFT, per-plane engines"
     return res
 

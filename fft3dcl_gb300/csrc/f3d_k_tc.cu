@@ -582,12 +582,15 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
   constexpr int kTcFilterBatch = filter_batch(MINB);
-  // Interleaved batches (outputs of one geometry, e.g. consecutive frames of
-  // a plane) run the same group of every output back to back, so that the
+  // A run of planes of one geometry (e.g. consecutive frames of a plane)
+  // runs the same group of each of its planes back to back, so that the
   // window spectra they share are read from L2 the second time.
-  const int pl = B.interleave ? (int)(blockIdx.x % B.n) : plane_of(B, B.cta0, blockIdx.x);
+  const int r0 = B.run[plane_of(B, B.cta0, blockIdx.x)];
+  const int rl = B.rlen[r0];
+  const int local = (int)blockIdx.x - B.cta0[r0];
+  const int pl = r0 + local % rl;
   const SweepArgs& sa = B.p[pl];
-  const int cta = B.interleave ? (int)(blockIdx.x / B.n) : (int)(blockIdx.x - B.cta0[pl]);
+  const int cta = local / rl;
   const InvArgs& a = sa.inv;
   extern __shared__ __align__(16) uint8_t smem_f[];
   float2* fbuf = reinterpret_cast<float2*>(smem_f);
@@ -613,7 +616,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   // windows (consecutive outputs, their CTAs side by side), each later output
   // pulls only its newest frame: the others are an earlier output's.
   constexpr uint32_t BIN_BYTES = HALF ? 4 : 8;
-  const bool pull = !B.shifted || pl == 0 || tid == NF - 1;
+  const bool pull = !((B.shifted >> pl) & 1) || tid == NF - 1;
   if (F3D_TC_FILTER_PREFETCH && tid < NF && nvbin > 0 && pull)
     tc::prefetch_l2(reinterpret_cast<const uint8_t*>(a.s[tid]) + gb0 * BIN_BYTES, (uint32_t)(nvbin * BIN_BYTES));
   if (tid < C::G) {
@@ -1029,17 +1032,22 @@ bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& B
     for (int i = n + 1; i <= kMaxBatch; i++) out.cta0[i] = out.cta0[n];
   };
   prefix(Bf, [](const SweepArgs& a) { return a.strips * (a.cells_y + 1); });  // (row, strip) groups
-  Bf.interleave = 1;
-  for (int i = 1; i < n; i++)
-    if (B.p[i].inv.g.W != B.p[0].inv.g.W || B.p[i].inv.g.H != B.p[0].inv.g.H || B.p[i].strips != B.p[0].strips)
-      Bf.interleave = 0;
-  // Consecutive outputs of one plane: every window frame but the newest is
-  // the previous entry's (the same spectrum buffers).
+  // Runs of consecutive planes of one geometry (the same group count). A run
+  // of consecutive outputs of one plane is shifted: every window frame but
+  // the newest is the previous entry's (the same spectrum buffers).
   const int nf = B.p[0].inv.bm >= 2 ? B.p[0].inv.bm : 1;
-  Bf.shifted = Bf.interleave && n > 1 && nf > 1;
-  for (int i = 1; i < n && Bf.shifted; i++)
-    for (int k = 0; k + 1 < nf; k++)
-      if (B.p[i].inv.s[k] != B.p[i - 1].inv.s[k + 1]) Bf.shifted = 0;
+  Bf.shifted = 0;
+  for (int i = 0; i < n; i++) {
+    const SweepArgs& a = B.p[i];
+    const bool same = i > 0 && a.inv.g.W == B.p[i - 1].inv.g.W && a.inv.g.H == B.p[i - 1].inv.g.H &&
+                      a.strips == B.p[i - 1].strips;
+    Bf.run[i] = same ? Bf.run[i - 1] : i;
+    Bf.rlen[i] = 0;
+    Bf.rlen[Bf.run[i]]++;
+    bool shift = same && nf > 1;
+    for (int k = 0; k + 1 < nf && shift; k++) shift = a.inv.s[k] == B.p[i - 1].inv.s[k + 1];
+    if (shift) Bf.shifted |= 1 << i;
+  }
   prefix(Bs, [](const SweepArgs& a) { return a.strips * a.segs; });          // (strip, segment)
   prefix(Bm, [](const SweepArgs& a) { return a.segs > 1 ? a.segs - 1 : 0; });  // seams
   return true;

@@ -172,8 +172,13 @@ struct TcFwdBatch {
 struct SweepBatch {
   int n;
   int cta0[kMaxBatch + 1];
-  int interleave;  // filter: planes of one geometry, CTA i is group i / n of plane i % n
-  int shifted;     // filter, interleaved: plane i's window is plane i-1's shifted by one frame
+  // Filter: runs of consecutive planes of one geometry. run[i] is the first
+  // plane of plane i's run, rlen[r] the length of the run starting at r; the
+  // run's CTAs interleave its planes (CTA j of the run: group j / rlen of
+  // plane r + j % rlen).
+  int run[kMaxBatch];
+  int rlen[kMaxBatch];
+  int shifted;  // filter: bit i set when plane i's window is plane i-1's (same run) moved on by one frame
   SweepArgs p[kMaxBatch];
 };
 // Launch shape of the tensor-core kernels, picked by the autotuner.

@@ -162,6 +162,53 @@ def test_lookahead_step_overlaps_and_equals_engines(flags):
             np.testing.assert_array_equal(g, r, err_msg=f"plane {i} frame {n}")
 
 
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("order", ["by_plane", "by_frame"])
+def test_yuv_two_frames_per_step_equal_engines(order, graph):
+    # Two consecutive YUV frames per step, six outputs of three engines. By
+    # plane ([Y, Y, U, U, V, V]) the filter runs two runs of one geometry
+    # (luma; both chroma planes), each interleaving its outputs' CTAs; by
+    # frame ([Y, U, V, Y, U, V]) the chroma pairs form the runs.
+    planes = yuv420(480, 272, 9, 27, 8)
+    params = dict(sigma=2.5, bt=4, sharpen=0.4, scutoff=0.3, svr=1.0, smin=4.0, smax=20.0)
+    ref, _ = run_planes(planes, params, [False, True, True], 8, None)
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.Stream(device=dev)
+    nfr = len(planes[0])
+    ip = F.validate(480, 272, 8, **params)
+    bt, cur = ip.bt, ip.current
+    engines = [F.Engine(p[0].shape[1], p[0].shape[0], 8, chroma=i > 0, form="tc", stream=st.cuda_stream,
+                        **params) for i, p in enumerate(planes)]
+    src = [torch.from_numpy(np.stack(p)).to(dev) for p in planes]
+    slots = [(i, r) for i in range(3) for r in range(2)] if order == "by_plane" else \
+            [(i, r) for r in range(2) for i in range(3)]
+    dst = [torch.empty(planes[i][0].shape, dtype=torch.uint8, device=dev) for i, _ in slots]
+    pitch = [planes[i][0].shape[1] for i, _ in slots]
+    b = F.Batch([engines[i] for i, _ in slots], graph=graph, autotune=True)
+    got = [[None] * nfr for _ in range(3)]
+    with torch.cuda.stream(st):
+        for n in range(0, nfr, 2):
+            wins = [[min(max(n + r - cur + k, 0), nfr - 1) for k in range(bt)] for _, r in slots]
+            for (i, _), win in zip(slots, wins):
+                for fn in win:
+                    if not engines[i].has(fn):
+                        engines[i].forward_device(fn, src[i][fn].data_ptr(), planes[i][0].shape[1])
+            b.step([-1] * len(slots), [src[i][0].data_ptr() for i, _ in slots], pitch, wins,
+                   [d.data_ptr() for d in dst], pitch)
+            st.synchronize()
+            for (i, r), d in zip(slots, dst):
+                if n + r < nfr:
+                    got[i][n + r] = d.cpu().numpy()
+            for e in engines:
+                e.prune(n - cur - 1, n + 2 - cur + bt)
+    b.close()
+    for e in engines:
+        e.close()
+    for i in range(3):
+        for n in range(nfr):
+            np.testing.assert_array_equal(got[i][n], ref[i][n], err_msg=f"plane {i} frame {n}")
+
+
 def test_mixed_sizes_batch_equals_engines():
     a = synth.moving_rects(640, 360, 6, 31, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
     b = synth.moving_rects(1000, 200, 6, 32, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
