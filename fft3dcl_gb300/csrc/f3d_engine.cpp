@@ -782,7 +782,7 @@ struct f3d_batch {
     cudaGraphExec_t x = nullptr;
     int kernels = 0;
   };
-  std::map<unsigned, Graph> graphs;  // by the planes with a forward (bits 0-7), an output (8-15), overlap (16)
+  std::map<uint64_t, Graph> graphs;  // by the planes with a forward (bits 0-15), an output (16-31), overlap (32)
   std::string err;
   // Side stream of the forward when it does not feed this step's outputs.
   cudaStream_t side = nullptr;
@@ -925,7 +925,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   TcFwdArgs fa[kMaxBatch];
   SweepArgs sa[kMaxBatch];
   int nf = 0;
-  unsigned mask = 0;
+  uint64_t mask = 0;
   for (int i = 0; i < n; i++) {
     f3d_engine* e = b->eng[i];
     if (fns[i] >= 0 && !e->cache.count(fns[i])) {
@@ -934,7 +934,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
       float2* spec = spectra_slot(e, fns[i], true);
       if (!spec) return batch_fail(b, F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
       fa[nf++] = tc_forward_args(e, static_cast<const uint8_t*>(dev_src[i]), (long long)src_pitch[i], e->fmt, spec);
-      mask |= 1u << i;
+      mask |= 1ull << i;
     }
   }
   int ns = 0;
@@ -953,7 +953,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
       sa[ns].seam_t = b->seam[i] ? b->seam[i] + (size_t)(sa[ns].segs - 1) * (a.g.bh / 2) * sa[ns].seam_w : nullptr;
     }
     ns++;
-    mask |= 1u << (8 + i);
+    mask |= 1ull << (16 + i);
   }
   if (nf == 0 && ns == 0) return F3D_OK;
   // When no plane's entering frame is in its own window (the caller runs one
@@ -962,12 +962,12 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   // stream at the end of the step (the next step's outputs need it).
   bool overlap = nf > 0 && ns > 0;
   for (int i = 0; i < n && overlap; i++)
-    if (fns[i] >= 0 && (mask & (1u << i)))
+    if (fns[i] >= 0 && (mask & (1ull << i)))
       for (int j = 0; j < n; j++)
         if (b->eng[j] == b->eng[i])
           for (int k = 0; k < nwin[j]; k++)
             if (windows[j][k] == fns[i]) overlap = false;
-  if (overlap) mask |= 1u << 16;
+  if (overlap) mask |= 1ull << 32;
   // Filter, inverse and seam merge; timed by events unless being captured.
   auto sweep = [&](const TcTune& t) -> cudaError_t {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1001,8 +1001,8 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   // result is the same for all of them; the last run leaves it in place),
   // and keep the one with the fastest run: with two runs, step-to-step noise
   // of about 1 % picked a filter variant 3 % slower at eight outputs.
-  const unsigned all = (1u << n) - 1;
-  if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFu) == (all | (all << 8))) {
+  const uint64_t all = (1ull << n) - 1;
+  if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFFFFFull) == (all | (all << 16))) {
     const TcTune cands[] = {{3, 5}, {2, 5}, {1, 5}, {3, 4}, {2, 4}, {1, 4}, {3, 3}, {2, 3}, {1, 3}};
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);

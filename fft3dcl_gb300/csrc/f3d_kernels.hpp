@@ -160,10 +160,10 @@ cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st);
 // of a YUV frame, or planes of several streams). A CTA finds its plane from
 // the prefix of per-plane CTA (forward: block-group) counts. Passed by value
 // as kernel parameters, so a captured CUDA graph is re-pointed at the next
-// frame's buffers by updating its kernel nodes' parameters. At 8 planes a
-// SweepBatch is about 6.6 KB: above the classic 4 KB parameter limit, within
+// frame's buffers by updating its kernel nodes' parameters. At 16 planes a
+// SweepBatch is about 13.5 KB: above the classic 4 KB parameter limit, within
 // the 32 KB that CUDA 12.1+ allows for __grid_constant__ parameters.
-constexpr int kMaxBatch = 8;
+constexpr int kMaxBatch = 16;
 struct TcFwdBatch {
   int n;
   int grp0[kMaxBatch + 1];

@@ -245,7 +245,7 @@ int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
                         size_t dst_pitch, void* stream);
 
 /* ---- Batches of planes -----------------------------------------------------
- * One temporal step of up to eight planes (the planes of a YUV frame,
+ * One temporal step of up to sixteen planes (the planes of a YUV frame,
  * planes of several streams, or consecutive outputs of one plane: the same
  * engine given several times) with one launch per kernel: the forward
  * transform of each plane's entering frame, then filter, inverse and

@@ -220,6 +220,13 @@ def test_mixed_sizes_batch_equals_engines():
             np.testing.assert_array_equal(g, r)
 
 
+def test_batch_holds_at_most_sixteen_entries():
+    with F.Engine(96, 64, 8, form="tc", bt=3) as e:
+        F.Batch([e] * 16).close()
+        with pytest.raises(F.F3DError):
+            F.Batch([e] * 17)
+
+
 def test_batch_rejects_mixed_forms():
     with F.Engine(96, 64, 8, form="tc", bt=3) as e1, F.Engine(96, 64, 8, form="fast", bt=3) as e2:
         with pytest.raises(F.F3DError):
@@ -265,7 +272,7 @@ def consecutive_outputs(frames, bits, params, k, graph, shape=None, flags=0):
 
 
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("k", [2, 4, 8])
+@pytest.mark.parametrize("k", [2, 4, 8, 16])
 def test_several_outputs_per_step_equal_engine(k, graph):
     frames = synth.moving_rects(320, 192, 13, 51, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
     params = dict(sigma=3.0, bt=4, sharpen=0.3)
