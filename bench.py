@@ -4,7 +4,7 @@
 Workload: 3840x2160 10-bit luma, sigma=3 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4
 precision=2, a seeded synthetic 48-frame clip (ramp + moving rectangles in
 64..940, Gaussian noise 12 LSB). One step of the tensor-core headline is one
-batch step of --outputs-per-step (default 8) consecutive output frames in
+batch step of --outputs-per-step (default 10) consecutive output frames in
 steady state: the forward transforms of the frames that enter the temporal
 window, then filter + inverse + overlap-add + 10-bit packing of each output.
 The other forms run one output frame per step.
@@ -48,9 +48,9 @@ NCU_TRAFFIC = {"tc": 571806464 + 130638592}
 # (k -> bytes): captured on the 1920x1080 case of this workload (`--size
 # 1920x1080 --steps 1 --warmup 3 --no-cpu --serve-streams 0 --no-yuv
 # --compare tc --outputs-per-step k`, mean of the k-output launches; k=4:
-# 260.2 MB read + 124.4 MB written, k=8: 410.5 + 286.0 MB) and scaled to
-# 3840x2160 by the block count (32912 / 8540).
-NCU_TRAFFIC_BATCH = {4: 1002927925 + 479516689, 8: 1581975962 + 1102231724}
+# 260.2 MB read + 124.4 MB written, k=8: 410.5 + 286.0 MB, k=10: 487.5 +
+# 365.7 MB) and scaled to 3840x2160 by the block count (32912 / 8540).
+NCU_TRAFFIC_BATCH = {4: 1002927925 + 479516689, 8: 1581975962 + 1102231724, 10: 1878657040 + 1409240147}
 
 
 def algorithmic_bytes(nb: int, fbw: int, bh: int, bt: int) -> dict:
@@ -644,7 +644,7 @@ def main():
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
     ap.add_argument("--no-batch", action="store_true",
                     help="tensor-core headline through the engine's own calls instead of a batch step")
-    ap.add_argument("--outputs-per-step", type=int, default=8, choices=list(range(1, 17)),
+    ap.add_argument("--outputs-per-step", type=int, default=10, choices=list(range(1, 17)),
                     help="tensor-core batch: consecutive output frames per step")
     ap.add_argument("--size", default=None,
                     help="WxH of the luma plane instead of 3840x2160 (small cases for profiling)")

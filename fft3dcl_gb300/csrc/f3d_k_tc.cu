@@ -76,9 +76,6 @@ struct TcCfg {
 };
 
 constexpr int kTcThreads = 256;
-#ifndef F3D_TC_FILTER_PREFETCH
-#define F3D_TC_FILTER_PREFETCH 1  // filter CTAs pull their group's spectra into L2 first
-#endif
 // Filter-kernel variants: CTAs per SM and the bins whose loads are in flight
 // together; fewer CTAs leave registers for deeper batches.
 __host__ __device__ constexpr int filter_batch(int minb) { return minb >= 5 ? 1 : (minb == 4 ? 2 : 4); }
@@ -617,7 +614,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   // pulls only its newest frame: the others are an earlier output's.
   constexpr uint32_t BIN_BYTES = HALF ? 4 : 8;
   const bool pull = !((B.shifted >> pl) & 1) || tid == NF - 1;
-  if (F3D_TC_FILTER_PREFETCH && tid < NF && nvbin > 0 && pull)
+  if (tid < NF && nvbin > 0 && pull)
     tc::prefetch_l2(reinterpret_cast<const uint8_t*>(a.s[tid]) + gb0 * BIN_BYTES, (uint32_t)(nvbin * BIN_BYTES));
   if (tid < C::G) {
     const int n = J0 + tid;
