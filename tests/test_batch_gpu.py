@@ -163,13 +163,13 @@ def test_lookahead_step_overlaps_and_equals_engines(flags):
 
 
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("order", ["by_plane", "by_frame"])
-def test_yuv_two_frames_per_step_equal_engines(order, graph):
-    # Two consecutive YUV frames per step, six outputs of three engines. By
-    # plane ([Y, Y, U, U, V, V]) the filter runs two runs of one geometry
-    # (luma; both chroma planes), each interleaving its outputs' CTAs; by
-    # frame ([Y, U, V, Y, U, V]) the chroma pairs form the runs.
-    planes = yuv420(480, 272, 9, 27, 8)
+@pytest.mark.parametrize("order,nf", [("by_plane", 2), ("by_frame", 2), ("by_plane", 4), ("by_plane", 5)])
+def test_yuv_frames_per_step_equal_engines(order, nf, graph):
+    # nf consecutive YUV frames per step, 3 nf outputs of three engines. By
+    # plane ([Y, Y, U, U, V, V] for two) the filter runs two runs of one
+    # geometry (luma; both chroma planes), each interleaving its outputs'
+    # CTAs; by frame ([Y, U, V, Y, U, V]) the chroma pairs form the runs.
+    planes = yuv420(480, 272, 11, 27, 8)
     params = dict(sigma=2.5, bt=4, sharpen=0.4, scutoff=0.3, svr=1.0, smin=4.0, smax=20.0)
     ref, _ = run_planes(planes, params, [False, True, True], 8, None)
     dev = torch.device("cuda", 0)
@@ -180,14 +180,14 @@ def test_yuv_two_frames_per_step_equal_engines(order, graph):
     engines = [F.Engine(p[0].shape[1], p[0].shape[0], 8, chroma=i > 0, form="tc", stream=st.cuda_stream,
                         **params) for i, p in enumerate(planes)]
     src = [torch.from_numpy(np.stack(p)).to(dev) for p in planes]
-    slots = [(i, r) for i in range(3) for r in range(2)] if order == "by_plane" else \
-            [(i, r) for r in range(2) for i in range(3)]
+    slots = [(i, r) for i in range(3) for r in range(nf)] if order == "by_plane" else \
+            [(i, r) for r in range(nf) for i in range(3)]
     dst = [torch.empty(planes[i][0].shape, dtype=torch.uint8, device=dev) for i, _ in slots]
     pitch = [planes[i][0].shape[1] for i, _ in slots]
     b = F.Batch([engines[i] for i, _ in slots], graph=graph, autotune=True)
     got = [[None] * nfr for _ in range(3)]
     with torch.cuda.stream(st):
-        for n in range(0, nfr, 2):
+        for n in range(0, nfr, nf):
             wins = [[min(max(n + r - cur + k, 0), nfr - 1) for k in range(bt)] for _, r in slots]
             for (i, _), win in zip(slots, wins):
                 for fn in win:
@@ -200,7 +200,7 @@ def test_yuv_two_frames_per_step_equal_engines(order, graph):
                 if n + r < nfr:
                     got[i][n + r] = d.cpu().numpy()
             for e in engines:
-                e.prune(n - cur - 1, n + 2 - cur + bt)
+                e.prune(n - cur - 1, n + nf - cur + bt)
     b.close()
     for e in engines:
         e.close()
