@@ -999,19 +999,22 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   // Autotuner: on the first step in which every plane enters a new frame,
   // time each candidate launch shape four times, interleaved (the step's
   // result is the same for all of them; the last run leaves it in place),
-  // and keep the one with the fastest run: with two runs, step-to-step noise
-  // of about 1 % picked a filter variant 3 % slower at eight outputs.
+  // and keep the one with the fastest run, the default unless that is more
+  // than 1 % slower: step-to-step noise of about 1 % picked a filter variant
+  // 1-3 % slower in steady state at eight and ten outputs.
   const uint64_t all = (1ull << n) - 1;
   if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFFFFFull) == (all | (all << 16))) {
     const TcTune cands[] = {{3, 5}, {2, 5}, {1, 5}, {3, 4}, {2, 4}, {1, 4}, {3, 3}, {2, 3}, {1, 3}};
+    constexpr int kCands = sizeof(cands) / sizeof(cands[0]);
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
     cudaEventCreate(&t1);
-    float best = 1e30f;
+    float fastest[kCands];
+    for (float& f : fastest) f = 1e30f;
     for (int rep = 0; rep < 4; rep++)
-      for (const TcTune& c : cands) {
+      for (int c = 0; c < kCands; c++) {
         cudaEventRecord(t0, b->stream);
-        cudaError_t ce = launch(c);
+        cudaError_t ce = launch(cands[c]);
         cudaEventRecord(t1, b->stream);
         if (ce == cudaSuccess) ce = cudaEventSynchronize(t1);
         if (ce != cudaSuccess) {
@@ -1021,13 +1024,17 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
         }
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, t0, t1);
-        if (ms < best) {
-          best = ms;
-          b->tune = c;
-        }
+        fastest[c] = std::min(fastest[c], ms);
       }
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
+    // The default shape (the first candidate) stays unless another is more
+    // than 1 % faster: single-step timings vary by about that much.
+    int pick = 0;
+    for (int c = 1; c < kCands; c++)
+      if (fastest[c] < fastest[pick]) pick = c;
+    if (fastest[0] <= 1.01f * fastest[pick]) pick = 0;
+    b->tune = cands[pick];
     b->tuned = true;
     std::lock_guard<std::mutex> lk(g_tune_mtx);
     g_tune_cache[tune_key(b)] = b->tune;

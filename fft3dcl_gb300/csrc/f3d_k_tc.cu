@@ -457,7 +457,11 @@ struct SwpCfg {
   using C = TcCfg<N>;
   static constexpr int TJ = C::G - 1;        // cells per strip
   static constexpr int CH = N / 2, CW = N / 2;
-  static constexpr int FS = C::PS + 4;       // filtered-bin stride per block (float2), padded
+  // Filtered-bin stride per block (float2), padded: in R a half-warp reads
+  // the same bin of 8 blocks for 2 k', which fall in 16 distinct bank pairs
+  // when FS / 2 is odd.
+  static constexpr int FS = C::PS + 2;
+  static_assert(FS % 4 == 2, "R-phase loads free of bank conflicts");
   static constexpr int PR = CW + 4;          // partial-sum row stride (floats), padded
   static constexpr int PC = CH * PR + 4;     // partial-sum cell stride (floats), padded
   static constexpr uint32_t TILE = 2 * C::A2_BYTES;                  // operand image: hi, lo
