@@ -473,7 +473,11 @@ struct SwpCfg {
   // A1, and the next tile is loaded once step 1' has read A1. Three CTAs fit
   // on an SM.
   static constexpr uint32_t A1 = A2;                                 // [tile][hi, lo] (INTERLEAVE)
-  static constexpr uint32_t P = A2 + TILE;                           // [2][TJ][PC] floats
+  // The second tile starts 64 B further than its hi + lo: in V the lanes of
+  // the two tiles store to the same offsets, which then fall in different
+  // banks.
+  static constexpr uint32_t A1_STRIDE = 2 * C::A1_BYTES + 64;
+  static constexpr uint32_t P = A2 + (C::T1 - 1) * A1_STRIDE + 2 * C::A1_BYTES;  // [2][TJ][PC] floats
   static constexpr uint32_t BAR = P + 2 * TJ * PC * 4;               // operand load, step 2', step 1'
   static constexpr uint32_t TSLOT = BAR + 24;
   static constexpr uint32_t BYTES = TSLOT + 8 + 1024;
@@ -481,7 +485,8 @@ struct SwpCfg {
   static constexpr uint32_t F_DC = C::G * FS * 8;
   static constexpr uint32_t F_BYTES = F_DC + C::G * 4;
   static_assert(C::T1 == 2, "one tile per block-column parity");
-  static_assert(2 * C::T1 * C::A1_BYTES <= TILE, "A1 fits the operand tile's space");
+  static_assert(P >= A2 + TILE, "the operand tile fits below the partial sums");
+  static_assert(A1_STRIDE % 16 == 0, "operand start addresses are 16-byte aligned");
   static_assert(BAR % 8 == 0 && P % 16 == 0, "alignment");
 };
 
@@ -750,7 +755,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
       const int r2 = 32 * s + lane;
       const int kp = r2 >> 3, bl = r2 & 7;
       const int tile = (J0 + bl) & 1, slot = bl >> 1;
-      uint8_t* t0 = sm + S::A1 + tile * 2 * C::A1_BYTES;
+      uint8_t* t0 = sm + S::A1 + tile * S::A1_STRIDE;
       float v[32];
       tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + 32 * h, v);
 #pragma unroll
@@ -773,7 +778,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
       constexpr uint32_t id1 = tc::idesc_f16(128, C::N1);
       const uint32_t sbo = (C::K1 / 8) * 128;
       for (int t = 0; t < C::T1; t++) {
-        const uint32_t a_hi = sbase + S::A1 + t * 2 * C::A1_BYTES, a_lo = a_hi + C::A1_BYTES;
+        const uint32_t a_hi = sbase + S::A1 + t * S::A1_STRIDE, a_lo = a_hi + C::A1_BYTES;
         const uint32_t b_hi = sbase + S::C1 + t * 2 * C::B1_BYTES, b_lo = b_hi + C::B1_BYTES;
         const uint32_t d = tmem + C::D1_COL + t * C::N1;
         for (int ks = 0; ks < C::K1 / 16; ks++) {
