@@ -585,7 +585,7 @@ BATCH_AUTOTUNE = 2
 
 
 class Batch:
-    """One temporal step of up to eight tensor-core engines (the planes of a
+    """One temporal step of up to sixteen tensor-core engines (the planes of a
     frame, planes of several streams, or one engine several times for
     consecutive outputs) with one launch per kernel
     (f3d_batch_*); optionally replayed as a CUDA graph and autotuned."""
