@@ -51,6 +51,9 @@ NCU_TRAFFIC = {"tc": 571806464 + 130638592}
 # 260.2 MB read + 124.4 MB written, k=8: 410.5 + 286.0 MB, k=10: 487.5 +
 # 365.7 MB) and scaled to 3840x2160 by the block count (32912 / 8540).
 NCU_TRAFFIC_BATCH = {4: 1002927925 + 479516689, 8: 1581975962 + 1102231724, 10: 1878657040 + 1409240147}
+# Consecutive outputs per batch step of the tensor-core headline (4K sweeps:
+# ten beat eight and twelve); its traffic must be in NCU_TRAFFIC_BATCH.
+DEFAULT_OUTPUTS_PER_STEP = 10
 
 
 def algorithmic_bytes(nb: int, fbw: int, bh: int, bt: int) -> dict:
@@ -644,7 +647,7 @@ def main():
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
     ap.add_argument("--no-batch", action="store_true",
                     help="tensor-core headline through the engine's own calls instead of a batch step")
-    ap.add_argument("--outputs-per-step", type=int, default=10, choices=list(range(1, 17)),
+    ap.add_argument("--outputs-per-step", type=int, default=DEFAULT_OUTPUTS_PER_STEP, choices=list(range(1, 17)),
                     help="tensor-core batch: consecutive output frames per step")
     ap.add_argument("--size", default=None,
                     help="WxH of the luma plane instead of 3840x2160 (small cases for profiling)")
