@@ -1,0 +1,71 @@
+// f3d_batch_plan.hpp -- host-side planning of the batched tensor-core
+// launches: the by-value batch parameters of the forward and of the filter,
+// inverse and seam-merge kernels, with each kernel's per-plane prefix of CTA
+// (or block-group) counts, the filter's runs of one geometry and its
+// shifted-window bits. Plain host code, also compiled by the CPU tests.
+#pragma once
+
+#include "f3d_kernels.hpp"
+
+namespace f3d {
+
+// Blocks per tensor-core forward group (one M = 128 tile of 8 blocks x 16
+// packed columns).
+constexpr int kTcGroupBlocks = 8;
+
+// The forward batch parameter of `planes` (false: not one batch).
+inline bool forward_batch(const TcFwdArgs* planes, int n, TcFwdBatch& B) {
+  if (n < 1 || n > kMaxBatch) return false;
+  B = TcFwdBatch{};
+  B.n = n;
+  for (int i = 0; i < n; i++) {
+    const TcFwdArgs& a = planes[i];
+    if (a.g.bw != 32 || a.g.bh != 32 || a.g.mode != 1 || a.fmt != planes[0].fmt) return false;
+    B.p[i] = a;
+    B.grp0[i + 1] = B.grp0[i] + (a.g.nb + kTcGroupBlocks - 1) / kTcGroupBlocks;
+  }
+  for (int i = n + 1; i <= kMaxBatch; i++) B.grp0[i] = B.grp0[n];
+  return true;
+}
+
+// The three sweep-side batch parameters (filter, inverse, seam merge) of
+// `planes`: the same planes, with the prefix of each kernel's CTA counts.
+inline bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& Bs, SweepBatch& Bm) {
+  if (n < 1 || n > kMaxBatch) return false;
+  SweepBatch B{};
+  B.n = n;
+  for (int i = 0; i < n; i++) {
+    const SweepArgs& a = planes[i];
+    if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm ||
+        a.inv.half != planes[0].inv.half)
+      return false;
+    B.p[i] = a;
+  }
+  auto prefix = [&](SweepBatch& out, auto count) {
+    out = B;
+    for (int i = 0; i < n; i++) out.cta0[i + 1] = out.cta0[i] + count(out.p[i]);
+    for (int i = n + 1; i <= kMaxBatch; i++) out.cta0[i] = out.cta0[n];
+  };
+  prefix(Bf, [](const SweepArgs& a) { return a.strips * (a.cells_y + 1); });  // (row, strip) groups
+  // Runs of consecutive planes of one geometry (the same group count). A run
+  // of consecutive outputs of one plane is shifted: every window frame but
+  // the newest is the previous entry's (the same spectrum buffers).
+  const int nf = B.p[0].inv.bm >= 2 ? B.p[0].inv.bm : 1;
+  Bf.shifted = 0;
+  for (int i = 0; i < n; i++) {
+    const SweepArgs& a = B.p[i];
+    const bool same = i > 0 && a.inv.g.W == B.p[i - 1].inv.g.W && a.inv.g.H == B.p[i - 1].inv.g.H &&
+                      a.strips == B.p[i - 1].strips;
+    Bf.run[i] = same ? Bf.run[i - 1] : i;
+    Bf.rlen[i] = 0;
+    Bf.rlen[Bf.run[i]]++;
+    bool shift = same && nf > 1;
+    for (int k = 0; k + 1 < nf && shift; k++) shift = a.inv.s[k] == B.p[i - 1].inv.s[k + 1];
+    if (shift) Bf.shifted |= 1 << i;
+  }
+  prefix(Bs, [](const SweepArgs& a) { return a.strips * a.segs; });          // (strip, segment)
+  prefix(Bm, [](const SweepArgs& a) { return a.segs > 1 ? a.segs - 1 : 0; });  // seams
+  return true;
+}
+
+}  // namespace f3d

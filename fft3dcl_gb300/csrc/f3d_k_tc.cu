@@ -26,6 +26,7 @@
 // B1hi + B1lo, or Xhi*B1hi + Xhi*B1lo + Xlo*B1hi; step 2 Ahi*Bhi + Ahi*Blo +
 // Alo*Bhi. The spectra of a group (8 x 4352 bytes, contiguous in HBM) leave
 // shared memory by one bulk copy.
+#include "f3d_batch_plan.hpp"
 #include "f3d_device.cuh"
 #include "f3d_tc.cuh"
 
@@ -994,6 +995,8 @@ std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<d
 
 bool tc_supported(int mode, int bw, int bh, int bm) { return mode == 1 && bw == 32 && bh == 32 && bm != 0; }
 
+static_assert(TcCfg<32>::G == kTcGroupBlocks, "forward group size of the batch plan");
+
 std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::vector<double>& wy,
                                const std::vector<double>& sxa, const std::vector<double>& sxb,
                                const std::vector<double>& sy) {
@@ -1001,62 +1004,6 @@ std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::
     if ((int)v->size() != n) return {};
   if (n == 32) return tables_n<32>(wx, wy, sxa, sxb, sy);
   return {};
-}
-
-// The forward batch parameter of `planes` (false: not one batch).
-bool forward_batch(const TcFwdArgs* planes, int n, TcFwdBatch& B) {
-  using C = TcCfg<32>;
-  if (n < 1 || n > kMaxBatch) return false;
-  B = TcFwdBatch{};
-  B.n = n;
-  for (int i = 0; i < n; i++) {
-    const TcFwdArgs& a = planes[i];
-    if (a.g.bw != 32 || a.g.bh != 32 || a.g.mode != 1 || a.fmt != planes[0].fmt) return false;
-    B.p[i] = a;
-    B.grp0[i + 1] = B.grp0[i] + (a.g.nb + C::G - 1) / C::G;
-  }
-  for (int i = n + 1; i <= kMaxBatch; i++) B.grp0[i] = B.grp0[n];
-  return true;
-}
-
-// The three sweep-side batch parameters (filter, inverse, seam merge) of
-// `planes`: the same planes, with the prefix of each kernel's CTA counts.
-bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& Bs, SweepBatch& Bm) {
-  if (n < 1 || n > kMaxBatch) return false;
-  SweepBatch B{};
-  B.n = n;
-  for (int i = 0; i < n; i++) {
-    const SweepArgs& a = planes[i];
-    if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm ||
-        a.inv.half != planes[0].inv.half)
-      return false;
-    B.p[i] = a;
-  }
-  auto prefix = [&](SweepBatch& out, auto count) {
-    out = B;
-    for (int i = 0; i < n; i++) out.cta0[i + 1] = out.cta0[i] + count(out.p[i]);
-    for (int i = n + 1; i <= kMaxBatch; i++) out.cta0[i] = out.cta0[n];
-  };
-  prefix(Bf, [](const SweepArgs& a) { return a.strips * (a.cells_y + 1); });  // (row, strip) groups
-  // Runs of consecutive planes of one geometry (the same group count). A run
-  // of consecutive outputs of one plane is shifted: every window frame but
-  // the newest is the previous entry's (the same spectrum buffers).
-  const int nf = B.p[0].inv.bm >= 2 ? B.p[0].inv.bm : 1;
-  Bf.shifted = 0;
-  for (int i = 0; i < n; i++) {
-    const SweepArgs& a = B.p[i];
-    const bool same = i > 0 && a.inv.g.W == B.p[i - 1].inv.g.W && a.inv.g.H == B.p[i - 1].inv.g.H &&
-                      a.strips == B.p[i - 1].strips;
-    Bf.run[i] = same ? Bf.run[i - 1] : i;
-    Bf.rlen[i] = 0;
-    Bf.rlen[Bf.run[i]]++;
-    bool shift = same && nf > 1;
-    for (int k = 0; k + 1 < nf && shift; k++) shift = a.inv.s[k] == B.p[i - 1].inv.s[k + 1];
-    if (shift) Bf.shifted |= 1 << i;
-  }
-  prefix(Bs, [](const SweepArgs& a) { return a.strips * a.segs; });          // (strip, segment)
-  prefix(Bm, [](const SweepArgs& a) { return a.segs > 1 ? a.segs - 1 : 0; });  // seams
-  return true;
 }
 
 cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st) {
@@ -1111,7 +1058,7 @@ cudaError_t launch_filter_h(const SweepBatch& B, int bm, cudaStream_t st) {
   }
 }
 
-// The planes of a batch share the spectrum storage (sweep_batches checks).
+// The planes of a batch store their spectra alike, fp32 or fp16 (sweep_batches checks).
 template <int MINB>
 cudaError_t launch_filter(const SweepBatch& B, int bm, cudaStream_t st) {
   return B.p[0].inv.half ? launch_filter_h<MINB, true>(B, bm, st) : launch_filter_h<MINB, false>(B, bm, st);
