@@ -68,4 +68,14 @@ inline bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepB
   return true;
 }
 
+// Autotuner choice among n timed launch shapes (fastest[i]: the fastest of
+// shape i's runs; shape 0 is the default): the fastest shape, unless the
+// default is within `margin` of it (single-step timings vary by about 1 %).
+inline int autotune_pick(const float* fastest, int n, float margin = 0.01f) {
+  int pick = 0;
+  for (int c = 1; c < n; c++)
+    if (fastest[c] < fastest[pick]) pick = c;
+  return fastest[0] <= (1.0f + margin) * fastest[pick] ? 0 : pick;
+}
+
 }  // namespace f3d

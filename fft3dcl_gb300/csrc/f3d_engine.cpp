@@ -10,6 +10,7 @@
 //   - the Kalman state for bt=0, resident across frames.
 // All device memory is counted in the process-wide live-bytes total.
 #include "f3d_host.hpp"
+#include "f3d_batch_plan.hpp"
 #include "f3d_kernels.hpp"
 
 #include <cuda_fp16.h>
@@ -1030,11 +1031,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
     cudaEventDestroy(t1);
     // The default shape (the first candidate) stays unless another is more
     // than 1 % faster: single-step timings vary by about that much.
-    int pick = 0;
-    for (int c = 1; c < kCands; c++)
-      if (fastest[c] < fastest[pick]) pick = c;
-    if (fastest[0] <= 1.01f * fastest[pick]) pick = 0;
-    b->tune = cands[pick];
+    b->tune = cands[autotune_pick(fastest, kCands)];
     b->tuned = true;
     std::lock_guard<std::mutex> lk(g_tune_mtx);
     g_tune_cache[tune_key(b)] = b->tune;

@@ -1,8 +1,8 @@
 // Host-side checks of the batched tensor-core launch plan
 // (fft3dcl_gb300/csrc/f3d_batch_plan.hpp): per-plane CTA prefixes, the
-// filter's runs of one geometry and its shifted-window bits, and the batches
-// the plan refuses. Built and run by tests/test_batch_plan_cpu.py; prints
-// "ok" or the first failed check.
+// filter's runs of one geometry and its shifted-window bits, the batches
+// the plan refuses, and the autotuner's choice. Built and run by
+// tests/test_batch_plan_cpu.py; prints "ok" or the first failed check.
 #include "f3d_batch_plan.hpp"
 
 #include <cstdio>
@@ -138,6 +138,13 @@ int main() {
     CHECK(B.grp0[kMaxBatch] == B.grp0[3]);
     f[2].fmt = FMT_U8;
     CHECK(!forward_batch(f, 3, B));
+  }
+  // Autotuner: the default shape (index 0) unless another is over 1 % faster.
+  {
+    const float same[3] = {1.0f, 1.0f, 1.0f}, close[3] = {1.0f, 0.995f, 1.2f}, clear[3] = {1.0f, 1.1f, 0.97f};
+    CHECK(autotune_pick(same, 3) == 0);
+    CHECK(autotune_pick(close, 3) == 0);
+    CHECK(autotune_pick(clear, 3) == 2);
   }
   if (!g_fail) std::printf("ok\n");
   return g_fail;
