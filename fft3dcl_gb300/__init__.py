@@ -416,7 +416,7 @@ class Filter:
         if fmt.sample_type == 0 and not 8 <= fmt.bits <= 16:
             raise ValueError("FFT3DCL: integer bit depths 8-16 only")
         if device == 0:
-            raise ValueError("FFT3DCL: device=0 (CPU backend) is not available in this build; "
+            raise ValueError("FFT3DCL: device=0 (CPU backend) is not available: there is no CPU path; "
                              "use device=1 or 2")
         self.clip = clip
         self.fmt = fmt

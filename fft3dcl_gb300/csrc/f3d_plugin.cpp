@@ -233,7 +233,7 @@ void VS_CC create(const VSMap* inmap, VSMap* out, void*, VSCore* core, const VSA
   sp.oldfft = (int)getI("oldfft", -1);
   const int device = (int)getI("device", 2);
   if (device == 0) {
-    vsapi->mapSetError(out, "FFT3DCL: device=0 (CPU backend) is not available in this build; use device=1 or 2");
+    vsapi->mapSetError(out, "FFT3DCL: device=0 (CPU backend) is not available: there is no CPU path; use device=1 or 2");
     return;
   }
 
