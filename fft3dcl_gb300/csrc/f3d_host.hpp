@@ -147,21 +147,22 @@ inline Grid make_grid(const f3d_internal_params& p) {
 
 constexpr double kPi = 3.14159265358979323846;
 
+// The table builders below write into caller storage and allocate nothing,
+// so that the no-alloc entry point (f3d_noalloc.cu) can use them with stack
+// storage; the vector-returning versions further down wrap them.
+
 // FftPlan twiddles, src/cpu/fft.cpp:8-14: exp(-2*pi*i*k/n) in double, stored
-// as float, k < n/2; interleaved re, im.
-inline std::vector<float> twiddles(int n) {
-  std::vector<float> tw(n);
+// as float, k < n/2; interleaved re, im (n floats).
+inline void twiddles_into(int n, float* tw) {
   for (int k = 0; k < n / 2; k++) {
     double a = -2.0 * 3.14159265358979323846 * k / n;
     tw[2 * k] = (float)std::cos(a);
     tw[2 * k + 1] = (float)std::sin(a);
   }
-  return tw;
 }
 
-// buildWindowMode0, src/cpu/tables.cpp:8-19.
-inline std::vector<float> window_mode0(int bw, int bh) {
-  std::vector<float> w(bw * bh);
+// buildWindowMode0, src/cpu/tables.cpp:8-19 (bw*bh floats).
+inline void window_mode0_into(int bw, int bh, float* w) {
   int off = 0;
   for (double n1 = -bh / 2.0 + 0.5; n1 < bh / 2.0; n1++) {
     double cosy = std::cos(n1 * kPi / bh);
@@ -170,98 +171,90 @@ inline std::vector<float> window_mode0(int bw, int bh) {
       w[off++] = (float)std::sqrt(0.5 * (cosx * cosx + cosy * cosy));
     }
   }
-  return w;
 }
 
-// buildWindowsMode1, src/cpu/tables.cpp:21-105, plus the odd-parity synthesis
-// window shifted by (bw-ow), src/cpu/reference.cpp:51-57.
-// The windows are separable: A[y][x] = float(ax[x] * ay[y]), synA[y][x] =
-// float(sxa[x] * sy[y]), synB[y][x] = float(sxb[x] * sy[y]) (sxb includes
-// the odd grid's shift).
-struct Mode1Axes {
-  std::vector<double> ax, ay, sxa, sxb, sy;
-};
-inline void windows_mode1(int bw, int bh, int ow, int oh, int wintype, std::vector<float>& A,
-                          std::vector<float>& synA, std::vector<float>& synB, Mode1Axes* axes = nullptr) {
-  std::vector<double> wanx(ow), wany(oh), wsynx(ow), wsyny(oh);
-  auto half_cos = [](int i, int o) { return std::cos(kPi * (i - o + 0.5) / (o * 2.0)); };
-  for (int i = 0; i < ow; i++) {
-    if (wintype == 1) {
-      wanx[i] = std::sqrt(half_cos(i, ow));
-      wsynx[i] = wanx[i] * wanx[i] * wanx[i];
-    } else if (wintype == 2) {
-      wanx[i] = 1.0;
-      wsynx[i] = half_cos(i, ow);
-      wsynx[i] *= wsynx[i];
-    } else {
-      wanx[i] = half_cos(i, ow);
-      wsynx[i] = wanx[i];
-    }
+// Ramp i (0 <= i < o) of the mode-1 analysis and synthesis windows of one
+// axis, src/cpu/tables.cpp:29-60.
+inline void mode1_ramp(int i, int o, int wintype, double& an, double& syn) {
+  const double hc = std::cos(kPi * (i - o + 0.5) / (o * 2.0));
+  if (wintype == 1) {
+    an = std::sqrt(hc);
+    syn = an * an * an;
+  } else if (wintype == 2) {
+    an = 1.0;
+    syn = hc;
+    syn *= syn;
+  } else {
+    an = hc;
+    syn = an;
   }
-  for (int i = 0; i < oh; i++) {
-    if (wintype == 1) {
-      wany[i] = std::sqrt(half_cos(i, oh));
-      wsyny[i] = wany[i] * wany[i] * wany[i];
-    } else if (wintype == 2) {
-      wany[i] = 1.0;
-      wsyny[i] = half_cos(i, oh);
-      wsyny[i] *= wsyny[i];
-    } else {
-      wany[i] = half_cos(i, oh);
-      wsyny[i] = wany[i];
-    }
-  }
-  // Rising ramp, flat middle, falling ramp; the odd grid's synthesis ramp
-  // runs the other way round.
-  std::vector<double> wxA(bw), wxSA(bw), wxSB(bw), wyA(bh), wySA(bh);
+}
+
+// Axis factors of the separable mode-1 windows, src/cpu/tables.cpp:62-105,
+// with the odd grid's synthesis shift of src/cpu/reference.cpp:51-57:
+// A[y][x] = float(ax[x] * ay[y]), synA[y][x] = float(sxa[x] * sy[y]),
+// synB[y][x] = float(sxb[x] * sy[y]). ax, sxa, sxb hold bw doubles, ay, sy bh.
+// Rising ramp, flat middle, falling ramp; the odd grid's synthesis ramp runs
+// the other way round, sampled (bw - ow) further along x.
+inline void mode1_axes_into(int bw, int bh, int ow, int oh, int wintype, double* ax, double* ay, double* sxa,
+                            double* sxb, double* sy) {
+  double an, syn;
   for (int lx = 0; lx < bw; lx++) {
     if (lx < ow) {
-      wxA[lx] = wanx[lx];
-      wxSA[lx] = wsynx[lx];
-      wxSB[lx] = wsynx[(ow - 1) - lx];
+      mode1_ramp(lx, ow, wintype, an, syn);
+      ax[lx] = an;
+      sxa[lx] = syn;
     } else if (lx < bw - ow) {
-      wxA[lx] = wxSA[lx] = wxSB[lx] = 1.0;
+      ax[lx] = sxa[lx] = 1.0;
     } else {
-      int x = lx - (bw - ow);
-      wxA[lx] = wanx[(ow - 1) - x];
-      wxSA[lx] = wsynx[(ow - 1) - x];
-      wxSB[lx] = wsynx[x];
+      mode1_ramp((ow - 1) - (lx - (bw - ow)), ow, wintype, an, syn);
+      ax[lx] = an;
+      sxa[lx] = syn;
+    }
+    // Odd-grid synthesis factor at lx' = (lx + bw - ow) % bw: wsynx[(ow-1)-lx']
+    // on the rising part, 1 in the middle, wsynx[lx' - (bw-ow)] on the falling part.
+    const int s = (lx + bw - ow) % bw;
+    if (s < ow) {
+      mode1_ramp((ow - 1) - s, ow, wintype, an, syn);
+      sxb[lx] = syn;
+    } else if (s < bw - ow) {
+      sxb[lx] = 1.0;
+    } else {
+      mode1_ramp(s - (bw - ow), ow, wintype, an, syn);
+      sxb[lx] = syn;
     }
   }
   for (int ly = 0; ly < bh; ly++) {
     if (ly < oh) {
-      wyA[ly] = wany[ly];
-      wySA[ly] = wsyny[ly];
+      mode1_ramp(ly, oh, wintype, an, syn);
+      ay[ly] = an;
+      sy[ly] = syn;
     } else if (ly < bh - oh) {
-      wyA[ly] = wySA[ly] = 1.0;
+      ay[ly] = sy[ly] = 1.0;
     } else {
-      wyA[ly] = wany[bh - 1 - ly];
-      wySA[ly] = wsyny[bh - 1 - ly];
+      mode1_ramp(bh - 1 - ly, oh, wintype, an, syn);
+      ay[ly] = an;
+      sy[ly] = syn;
     }
   }
-  if (axes) {
-    // synB below is sb shifted cyclically by bw - ow along x.
-    std::vector<double> sxb(bw);
-    for (int lx = 0; lx < bw; lx++) sxb[lx] = wxSB[(lx + bw - ow) % bw];
-    *axes = Mode1Axes{wxA, wyA, wxSA, sxb, wySA};
-  }
-  A.assign(bw * bh, 0.0f);
-  synA.assign(bw * bh, 0.0f);
-  std::vector<float> sb(bw * bh);
-  for (int ly = 0; ly < bh; ly++)
-    for (int lx = 0; lx < bw; lx++) {
-      A[ly * bw + lx] = (float)(wxA[lx] * wyA[ly]);
-      synA[ly * bw + lx] = (float)(wxSA[lx] * wySA[ly]);
-      sb[ly * bw + lx] = (float)(wxSB[lx] * wySA[ly]);
-    }
-  synB.assign(bw * bh, 0.0f);
-  for (int ly = 0; ly < bh; ly++)
-    for (int lx = 0; lx < bw; lx++) synB[ly * bw + lx] = sb[ly * bw + ((lx + bw - ow) % bw)];
 }
 
-// buildPattern, src/cpu/tables.cpp:107-137 (float arithmetic as there).
-inline std::vector<float> sigma_pattern(int bw, int bh, int bt, float sigma, float sigma2,
-                                        float sigma3, float sigma4) {
+// buildWindowsMode1, src/cpu/tables.cpp:21-105, from the axis factors
+// (bw*bh floats each).
+inline void windows_mode1_into(int bw, int bh, const double* ax, const double* ay, const double* sxa,
+                               const double* sxb, const double* sy, float* A, float* synA, float* synB) {
+  for (int ly = 0; ly < bh; ly++)
+    for (int lx = 0; lx < bw; lx++) {
+      A[ly * bw + lx] = (float)(ax[lx] * ay[ly]);
+      synA[ly * bw + lx] = (float)(sxa[lx] * sy[ly]);
+      synB[ly * bw + lx] = (float)(sxb[lx] * sy[ly]);
+    }
+}
+
+// buildPattern, src/cpu/tables.cpp:107-137 (float arithmetic as there;
+// (bw/2+1)*bh floats).
+inline void sigma_pattern_into(int bw, int bh, int bt, float sigma, float sigma2, float sigma3, float sigma4,
+                               float* pat) {
   const int fbw = bw / 2 + 1;
   auto scale = [&](float s) {
     double v = s / 255.0;
@@ -270,7 +263,6 @@ inline std::vector<float> sigma_pattern(int bw, int bh, int bt, float sigma, flo
   float s = scale(sigma), s2 = scale(sigma2), s3 = scale(sigma3), s4 = scale(sigma4);
   float ft2 = (float)(std::sqrt(0.5) / 2.0);
   float ft3 = (float)(std::sqrt(0.5) / 4.0);
-  std::vector<float> pat(fbw * bh);
   for (int h = 0; h < bh; h++) {
     float fy = (bh - 2.0f * std::fabs(h - bh / 2.0f)) / bh;
     for (int w = 0; w < fbw; w++) {
@@ -286,13 +278,11 @@ inline std::vector<float> sigma_pattern(int bw, int bh, int bt, float sigma, flo
       pat[h * fbw + w] = p;
     }
   }
-  return pat;
 }
 
-// buildSharpenLUT, src/cpu/tables.cpp:139-156.
-inline std::vector<float> sharpen_lut(int bw, int bh, float strength, float svr, float scutoff) {
+// buildSharpenLUT, src/cpu/tables.cpp:139-156 ((bw/2+1)*bh floats).
+inline void sharpen_lut_into(int bw, int bh, float strength, float svr, float scutoff, float* lut) {
   const int fbw = bw / 2 + 1;
-  std::vector<float> lut(fbw * bh);
   for (int j = 0; j < bh; j++) {
     int dj = j >= bh / 2 ? bh - j : j;
     float d2v = (float)(dj * dj) * (svr * svr) / ((bh / 2.0f) * (bh / 2.0f));
@@ -301,13 +291,17 @@ inline std::vector<float> sharpen_lut(int bw, int bh, float strength, float svr,
       lut[j * fbw + i] = strength * (1.0f - std::exp(-d2 / (2.0f * scutoff * scutoff)));
     }
   }
-  return lut;
 }
+
+// Largest transform length the host transform below takes (the reference
+// rounds block sizes to at most 512, src/params.h:62-72).
+constexpr int kMaxHostFft = 512;
 
 // Reference radix-2 DIT transform (src/cpu/fft.cpp:28-58) on the host, used
 // once per engine to build the degrid sample the same way the reference does.
-inline void host_fft(int n, const std::vector<float>& tw, const float* in, float* out, bool inv) {
-  std::vector<float> a(2 * n);
+// tw: interleaved twiddles of length n; in, out: n interleaved complex values.
+inline void host_fft(int n, const float* tw, const float* in, float* out, bool inv) {
+  float a[2 * kMaxHostFft];
   int bits = 0;
   while ((1 << bits) < n) bits++;
   for (int i = 0; i < n; i++) {
@@ -339,36 +333,92 @@ inline void host_fft(int n, const std::vector<float>& tw, const float* in, float
 // buildDegridSample, src/cpu/reference.cpp:172-198: FFT of the analysis
 // window (the reference transforms a white frame, whose blocks all equal the
 // window) divided by its DC and scaled by degrid. One fbw x bh table serves
-// every block. Interleaved re, im.
-inline std::vector<float> degrid_sample(int bw, int bh, float degrid, const std::vector<float>& win) {
+// every block; gs receives 2*fbw*bh floats, interleaved re, im. The row
+// transforms keep their fbw columns and only those columns are transformed
+// (column transforms are independent of each other).
+inline void degrid_sample_into(int bw, int bh, float degrid, const float* win, const float* tw_row,
+                               const float* tw_col, float* gs) {
   const int fbw = bw / 2 + 1;
-  std::vector<float> twr = twiddles(bw), twc = twiddles(bh);
-  std::vector<float> full(2 * bw * bh), row(2 * bw), col(2 * bh), colout(2 * bh);
+  float buf[2 * kMaxHostFft], res[2 * kMaxHostFft];
   for (int r = 0; r < bh; r++) {
     for (int c = 0; c < bw; c++) {
-      row[2 * c] = win[r * bw + c];
-      row[2 * c + 1] = 0.0f;
+      buf[2 * c] = win[r * bw + c];
+      buf[2 * c + 1] = 0.0f;
     }
-    host_fft(bw, twr, row.data(), &full[2 * r * bw], false);
+    host_fft(bw, tw_row, buf, res, false);
+    for (int c = 0; c < fbw; c++) {
+      gs[2 * (r * fbw + c)] = res[2 * c];
+      gs[2 * (r * fbw + c) + 1] = res[2 * c + 1];
+    }
   }
   for (int c = 0; c < fbw; c++) {
     for (int r = 0; r < bh; r++) {
-      col[2 * r] = full[2 * (r * bw + c)];
-      col[2 * r + 1] = full[2 * (r * bw + c) + 1];
+      buf[2 * r] = gs[2 * (r * fbw + c)];
+      buf[2 * r + 1] = gs[2 * (r * fbw + c) + 1];
     }
-    host_fft(bh, twc, col.data(), colout.data(), false);
+    host_fft(bh, tw_col, buf, res, false);
     for (int r = 0; r < bh; r++) {
-      full[2 * (r * bw + c)] = colout[2 * r];
-      full[2 * (r * bw + c) + 1] = colout[2 * r + 1];
+      gs[2 * (r * fbw + c)] = res[2 * r];
+      gs[2 * (r * fbw + c) + 1] = res[2 * r + 1];
     }
   }
-  std::vector<float> gs(2 * fbw * bh);
-  const float dc = full[0];
-  for (int r = 0; r < bh; r++)
-    for (int c = 0; c < fbw; c++) {
-      gs[2 * (r * fbw + c)] = full[2 * (r * bw + c)] / dc * degrid;
-      gs[2 * (r * fbw + c) + 1] = full[2 * (r * bw + c) + 1] / dc * degrid;
-    }
+  const float dc = gs[0];
+  for (int i = 0; i < fbw * bh; i++) {
+    gs[2 * i] = gs[2 * i] / dc * degrid;
+    gs[2 * i + 1] = gs[2 * i + 1] / dc * degrid;
+  }
+}
+
+// ---- vector-returning wrappers (the engine) ---------------------------------
+
+inline std::vector<float> twiddles(int n) {
+  std::vector<float> tw(n);
+  twiddles_into(n, tw.data());
+  return tw;
+}
+
+inline std::vector<float> window_mode0(int bw, int bh) {
+  std::vector<float> w(bw * bh);
+  window_mode0_into(bw, bh, w.data());
+  return w;
+}
+
+struct Mode1Axes {
+  std::vector<double> ax, ay, sxa, sxb, sy;
+};
+inline Mode1Axes mode1_axes(int bw, int bh, int ow, int oh, int wintype) {
+  Mode1Axes a{std::vector<double>(bw), std::vector<double>(bh), std::vector<double>(bw),
+              std::vector<double>(bw), std::vector<double>(bh)};
+  mode1_axes_into(bw, bh, ow, oh, wintype, a.ax.data(), a.ay.data(), a.sxa.data(), a.sxb.data(), a.sy.data());
+  return a;
+}
+inline void windows_mode1(int bw, int bh, int ow, int oh, int wintype, std::vector<float>& A,
+                          std::vector<float>& synA, std::vector<float>& synB, Mode1Axes* axes = nullptr) {
+  const Mode1Axes a = mode1_axes(bw, bh, ow, oh, wintype);
+  A.assign(bw * bh, 0.0f);
+  synA.assign(bw * bh, 0.0f);
+  synB.assign(bw * bh, 0.0f);
+  windows_mode1_into(bw, bh, a.ax.data(), a.ay.data(), a.sxa.data(), a.sxb.data(), a.sy.data(), A.data(),
+                     synA.data(), synB.data());
+  if (axes) *axes = a;
+}
+
+inline std::vector<float> sigma_pattern(int bw, int bh, int bt, float sigma, float sigma2, float sigma3,
+                                        float sigma4) {
+  std::vector<float> pat((bw / 2 + 1) * bh);
+  sigma_pattern_into(bw, bh, bt, sigma, sigma2, sigma3, sigma4, pat.data());
+  return pat;
+}
+
+inline std::vector<float> sharpen_lut(int bw, int bh, float strength, float svr, float scutoff) {
+  std::vector<float> lut((bw / 2 + 1) * bh);
+  sharpen_lut_into(bw, bh, strength, svr, scutoff, lut.data());
+  return lut;
+}
+
+inline std::vector<float> degrid_sample(int bw, int bh, float degrid, const std::vector<float>& win) {
+  std::vector<float> gs(2 * (bw / 2 + 1) * bh), twr = twiddles(bw), twc = twiddles(bh);
+  degrid_sample_into(bw, bh, degrid, win.data(), twr.data(), twc.data(), gs.data());
   return gs;
 }
 

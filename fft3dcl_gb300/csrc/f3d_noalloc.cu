@@ -1,20 +1,26 @@
 // f3d_noalloc.cu -- f3d_denoise_noalloc: one frame through the exact-form
 // kernels with every intermediate in a static device array, for callers that
-// cannot call cudaMalloc (graph capture, fixed device-memory budgets,
-// real-time threads that must not take cudaMalloc's device-wide sync).
+// cannot call cudaMalloc (hosts that hand out a fixed device-memory budget up
+// front, real-time threads that must not take cudaMalloc/cudaFree's
+// device-wide synchronisation).
 //
 // Scratch layout (one call): [tables][window spectra x nwin][windowed blocks],
 // each region 256-byte aligned. Every byte the kernels read is written
-// earlier in the same call (tables by the upload, spectra by the forward
-// kernel, blocks by the inverse kernel), so nothing needs clearing between
-// calls.
+// earlier in the same call and on the same stream (tables by the table
+// kernel, spectra by the forward kernel, blocks by the inverse kernel), so
+// nothing needs clearing between calls.
+//
+// The tables are built on the host by the engine's own builders
+// (f3d_host.hpp) into stack storage and reach the device as parameters of
+// k_noalloc_tables: the launch copies them, so no host buffer has to outlive
+// the call and calls share no host staging.
 #include "f3d_host.hpp"
 #include "f3d_kernels.hpp"
 
 #include <cuda_runtime.h>
 
-#include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 
 namespace f3d {
@@ -29,21 +35,40 @@ using namespace f3d;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[F3D_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
-constexpr int kMaxDim = 64;               // block sizes of the GPU path
+constexpr int kMaxDim = 64;               // block sizes of this entry point
 constexpr int kMaxBins = (kMaxDim / 2 + 1) * kMaxDim;
 constexpr size_t kAlign = 256;
 
-std::mutex g_mtx;                          // guards the set-up and the host table staging
-unsigned char* g_scratch_ptr[kMaxDevices]; // device address of the array, per device
+// Host tables of one call, in their device order:
+// [win_ana | syn_a | syn_b | pattern | sharpen | gs].
+constexpr int kMaxTabFloats = 3 * kMaxDim * kMaxDim + 4 * kMaxBins;
 
-// Host staging of the tables, in the order they are laid out on the device.
-struct HostTables {
-  float win[3 * kMaxDim * kMaxDim];  // analysis, synthesis A, synthesis B
-  float pattern[kMaxBins];
-  float sharpen[kMaxBins];
-  float gs[2 * kMaxBins];            // degrid sample, interleaved re, im
+// One piece of the tables as a kernel parameter, within CUDA's 32 KB of
+// kernel parameters.
+constexpr int kPieceFloats = 7680;
+struct TablePiece {
+  float* dst;
+  int n;
+  float v[kPieceFloats];
 };
-HostTables g_host;
+static_assert(sizeof(TablePiece) <= 31 * 1024, "kernel parameter space");
+
+__global__ void k_noalloc_tables(const __grid_constant__ TablePiece p) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += gridDim.x * blockDim.x) p.dst[i] = p.v[i];
+}
+
+// Device address of the scratch array, looked up with cudaGetSymbolAddress
+// once per device and CUDA context, with that device current. The context is
+// part of the key: after cudaDeviceReset the runtime creates a new primary
+// context, in which the array has a new address.
+using CtxGetCurrent = int (*)(void**);  // cuCtxGetCurrent
+struct ScratchAddr {
+  void* ctx = nullptr;
+  unsigned char* ptr = nullptr;
+};
+std::mutex g_mtx;  // guards g_addr and g_ctx_get_current
+ScratchAddr g_addr[kMaxDevices];
+CtxGetCurrent g_ctx_get_current = nullptr;
 
 size_t round_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
@@ -52,207 +77,68 @@ int fail(int code, const char* msg) {
   return code;
 }
 
-// The table formulas below are the engine's (f3d_host.hpp, which restates
-// src/cpu/tables.cpp, src/cpu/fft.cpp:8-58 and src/cpu/reference.cpp:51-57,
-// 172-198) with stack storage instead of vectors; the GPU test of this entry
-// point checks that its output has the engine's bits.
-
-void twiddles_into(int n, float2* tw) {
-  for (int k = 0; k < n / 2; k++) {
-    double a = -2.0 * 3.14159265358979323846 * k / n;
-    tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
-  }
+void* current_context() {
+  void* ctx = nullptr;
+  if (g_ctx_get_current) g_ctx_get_current(&ctx);
+  return ctx;
 }
 
-void window_mode0_into(int bw, int bh, float* w) {
-  int off = 0;
-  for (double n1 = -bh / 2.0 + 0.5; n1 < bh / 2.0; n1++) {
-    double cosy = std::cos(n1 * kPi / bh);
-    for (double n2 = -bw / 2.0 + 0.5; n2 < bw / 2.0; n2++) {
-      double cosx = std::cos(n2 * kPi / bw);
-      w[off++] = (float)std::sqrt(0.5 * (cosx * cosx + cosy * cosy));
-    }
-  }
-}
-
-void ramps(int o, int wintype, double* wan, double* wsyn) {
-  for (int i = 0; i < o; i++) {
-    const double hc = std::cos(kPi * (i - o + 0.5) / (o * 2.0));
-    if (wintype == 1) {
-      wan[i] = std::sqrt(hc);
-      wsyn[i] = wan[i] * wan[i] * wan[i];
-    } else if (wintype == 2) {
-      wan[i] = 1.0;
-      wsyn[i] = hc;
-      wsyn[i] *= wsyn[i];
-    } else {
-      wan[i] = hc;
-      wsyn[i] = wan[i];
-    }
-  }
-}
-
-void windows_mode1_into(int bw, int bh, int ow, int oh, int wintype, float* A, float* synA, float* synB) {
-  double wanx[kMaxDim], wsynx[kMaxDim], wany[kMaxDim], wsyny[kMaxDim];
-  double wxA[kMaxDim], wxSA[kMaxDim], wxSB[kMaxDim], wyA[kMaxDim], wySA[kMaxDim];
-  ramps(ow, wintype, wanx, wsynx);
-  ramps(oh, wintype, wany, wsyny);
-  for (int lx = 0; lx < bw; lx++) {
-    if (lx < ow) {
-      wxA[lx] = wanx[lx];
-      wxSA[lx] = wsynx[lx];
-      wxSB[lx] = wsynx[(ow - 1) - lx];
-    } else if (lx < bw - ow) {
-      wxA[lx] = wxSA[lx] = wxSB[lx] = 1.0;
-    } else {
-      const int x = lx - (bw - ow);
-      wxA[lx] = wanx[(ow - 1) - x];
-      wxSA[lx] = wsynx[(ow - 1) - x];
-      wxSB[lx] = wsynx[x];
-    }
-  }
-  for (int ly = 0; ly < bh; ly++) {
-    if (ly < oh) {
-      wyA[ly] = wany[ly];
-      wySA[ly] = wsyny[ly];
-    } else if (ly < bh - oh) {
-      wyA[ly] = wySA[ly] = 1.0;
-    } else {
-      wyA[ly] = wany[bh - 1 - ly];
-      wySA[ly] = wsyny[bh - 1 - ly];
-    }
-  }
-  for (int ly = 0; ly < bh; ly++)
-    for (int lx = 0; lx < bw; lx++) {
-      A[ly * bw + lx] = (float)(wxA[lx] * wyA[ly]);
-      synA[ly * bw + lx] = (float)(wxSA[lx] * wySA[ly]);
-      const int sx = (lx + bw - ow) % bw;  // odd-parity window sampled (bw-ow) right
-      synB[ly * bw + lx] = (float)(wxSB[sx] * wySA[ly]);
-    }
-}
-
-void pattern_into(int bw, int bh, int bt, float sigma, float sigma2, float sigma3, float sigma4, float* pat) {
-  const int fbw = bw / 2 + 1;
-  auto scale = [&](float s) {
-    double v = s / 255.0;
-    return (float)(v * v * bt * bw * bh);
-  };
-  float s = scale(sigma), s2 = scale(sigma2), s3 = scale(sigma3), s4 = scale(sigma4);
-  float ft2 = (float)(std::sqrt(0.5) / 2.0);
-  float ft3 = (float)(std::sqrt(0.5) / 4.0);
-  for (int h = 0; h < bh; h++) {
-    float fy = (bh - 2.0f * std::fabs(h - bh / 2.0f)) / bh;
-    for (int w = 0; w < fbw; w++) {
-      float fx = w * 1.0f / fbw;
-      float f = std::sqrt((fx * fx + fy * fy) * 0.5f);
-      float p;
-      if (f < ft3)
-        p = s4 + (s3 - s4) * f / ft3;
-      else if (f < ft2)
-        p = s3 + (s2 - s3) * (f - ft3) / (ft2 - ft3);
-      else
-        p = s + (s2 - s) * (1.0f - f) / (1.0f - ft2);
-      pat[h * fbw + w] = p;
-    }
-  }
-}
-
-void sharpen_into(int bw, int bh, float strength, float svr, float scutoff, float* lut) {
-  const int fbw = bw / 2 + 1;
-  for (int j = 0; j < bh; j++) {
-    int dj = j >= bh / 2 ? bh - j : j;
-    float d2v = (float)(dj * dj) * (svr * svr) / ((bh / 2.0f) * (bh / 2.0f));
-    for (int i = 0; i < fbw; i++) {
-      float d2 = d2v + (float)(i * i) / ((bw / 2.0f) * (bw / 2.0f));
-      lut[j * fbw + i] = strength * (1.0f - std::exp(-d2 / (2.0f * scutoff * scutoff)));
-    }
-  }
-}
-
-// Radix-2 DIT of n interleaved complex values, forward (src/cpu/fft.cpp:28-58).
-void fft_forward(int n, const float2* tw, const float* in, float* out) {
-  float a[2 * kMaxDim];
-  int bits = 0;
-  while ((1 << bits) < n) bits++;
-  for (int i = 0; i < n; i++) {
-    int r = 0;
-    for (int b = 0; b < bits; b++)
-      if (i & (1 << b)) r |= 1 << (bits - 1 - b);
-    a[2 * i] = in[2 * r];
-    a[2 * i + 1] = in[2 * r + 1];
-  }
-  for (int len = 2; len <= n; len <<= 1) {
-    const int half = len >> 1, step = n / len;
-    for (int i = 0; i < n; i += len)
-      for (int j = 0; j < half; j++) {
-        const float wr = tw[j * step].x, wi = tw[j * step].y;
-        const float br = a[2 * (i + j + half)], bi = a[2 * (i + j + half) + 1];
-        const float tr = wr * br - wi * bi, ti = wr * bi + wi * br;
-        const float ur = a[2 * (i + j)], ui = a[2 * (i + j) + 1];
-        a[2 * (i + j)] = ur + tr;
-        a[2 * (i + j) + 1] = ui + ti;
-        a[2 * (i + j + half)] = ur - tr;
-        a[2 * (i + j + half) + 1] = ui - ti;
-      }
-  }
-  for (int i = 0; i < 2 * n; i++) out[i] = a[i];
-}
-
-// FFT of the analysis window / its DC x degrid; only the fbw kept columns
-// are transformed (column transforms are independent).
-void degrid_into(int bw, int bh, float degrid, const float* win, const float2* twr, const float2* twc,
-                 float* gs) {
-  const int fbw = bw / 2 + 1;
-  float row[2 * kMaxDim], res[2 * kMaxDim], col[2 * kMaxDim];
-  for (int r = 0; r < bh; r++) {
-    for (int c = 0; c < bw; c++) {
-      row[2 * c] = win[r * bw + c];
-      row[2 * c + 1] = 0.0f;
-    }
-    fft_forward(bw, twr, row, res);
-    for (int c = 0; c < fbw; c++) {
-      gs[2 * (r * fbw + c)] = res[2 * c];
-      gs[2 * (r * fbw + c) + 1] = res[2 * c + 1];
-    }
-  }
-  for (int c = 0; c < fbw; c++) {
-    for (int r = 0; r < bh; r++) {
-      col[2 * r] = gs[2 * (r * fbw + c)];
-      col[2 * r + 1] = gs[2 * (r * fbw + c) + 1];
-    }
-    fft_forward(bh, twc, col, res);
-    for (int r = 0; r < bh; r++) {
-      gs[2 * (r * fbw + c)] = res[2 * r];
-      gs[2 * (r * fbw + c) + 1] = res[2 * r + 1];
-    }
-  }
-  const float dc = gs[0];
-  for (int i = 0; i < fbw * bh; i++) {
-    gs[2 * i] = gs[2 * i] / dc * degrid;
-    gs[2 * i + 1] = gs[2 * i + 1] / dc * degrid;
-  }
-}
-
-// Device address of the scratch array on the current device, looked up once
-// per device with that device current.
 int scratch_on_current_device(unsigned char** out) {
   int dev = 0;
   cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) return fail(F3D_E_CUDA, "FFT3DCL: no current CUDA device for the no-alloc call");
   if (dev < 0 || dev >= kMaxDevices) return fail(F3D_E_UNSUPPORTED, "FFT3DCL: device ordinal above 63");
-  if (!g_scratch_ptr[dev]) {
+  std::lock_guard<std::mutex> lock(g_mtx);
+  if (!g_ctx_get_current) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_current = reinterpret_cast<CtxGetCurrent>(fn);
+    cudaGetLastError();
+  }
+  ScratchAddr& a = g_addr[dev];
+  void* ctx = current_context();
+  // A thread that has not used the runtime yet has no current context: the
+  // lookup below binds the device's context, and the key is taken after it.
+  if (!a.ptr || !ctx || ctx != a.ctx) {
     void* p = nullptr;
     ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (ce != cudaSuccess || !p) {
       char msg[200];
       std::snprintf(msg, sizeof msg, "FFT3DCL: cudaGetSymbolAddress of the no-alloc scratch failed: %s",
                     cudaGetErrorString(ce));
+      cudaGetLastError();
       return fail(F3D_E_CUDA, msg);
     }
-    g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+    a.ptr = static_cast<unsigned char*>(p);
+    a.ctx = current_context();
   }
-  *out = g_scratch_ptr[dev];
+  *out = a.ptr;
   return F3D_OK;
+}
+
+// Host tables of one call into t (kMaxTabFloats floats, the caller's stack).
+void build_tables_into(const f3d_internal_params& ip, const float* tw_row, const float* tw_col, float* t) {
+  const int bwbh = ip.bw * ip.bh, ps = (ip.bw / 2 + 1) * ip.bh;
+  float* ana = t;
+  float* sa = ana + bwbh;
+  float* sb = sa + bwbh;
+  float* pat = sb + bwbh;
+  float* shp = pat + ps;
+  float* gs = shp + ps;
+  std::memset(t, 0, sizeof(float) * (3 * (size_t)bwbh + 4 * (size_t)ps));
+  if (ip.mode == 0) {
+    window_mode0_into(ip.bw, ip.bh, ana);
+  } else {
+    double ax[kMaxDim], ay[kMaxDim], sxa[kMaxDim], sxb[kMaxDim], sy[kMaxDim];
+    mode1_axes_into(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, ax, ay, sxa, sxb, sy);
+    windows_mode1_into(ip.bw, ip.bh, ax, ay, sxa, sxb, sy, ana, sa, sb);
+  }
+  if (ip.use_pattern)
+    sigma_pattern_into(ip.bw, ip.bh, ip.bt, ip.sigma * 255.0f, ip.sigma2, ip.sigma3, ip.sigma4, pat);
+  if (ip.sharpen_on) sharpen_lut_into(ip.bw, ip.bh, ip.sharpen, ip.svr, ip.scutoff, shp);
+  if (ip.degrid_on) degrid_sample_into(ip.bw, ip.bh, ip.degrid, ana, tw_row, tw_col, gs);
 }
 
 }  // namespace
@@ -271,8 +157,8 @@ extern "C" int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_
   if (ip.bm == 0)
     return fail(F3D_E_UNSUPPORTED, "FFT3DCL: the no-alloc call has no state across frames; Kalman (bt=0) "
                                    "needs an engine");
-  if (!form_supported(F3D_FORM_EXACT, ip.bw, ip.bh))
-    return fail(F3D_E_UNSUPPORTED, "FFT3DCL: block size not supported by the GPU path (powers of two 4..64)");
+  if (ip.bw > kMaxDim || ip.bh > kMaxDim || !form_supported(F3D_FORM_EXACT, ip.bw, ip.bh))
+    return fail(F3D_E_UNSUPPORTED, "FFT3DCL: the no-alloc call takes block sizes 4..64");
   const int need = ip.bm >= 2 ? ip.bt : 1;
   if (nwin != need) {
     char msg[120];
@@ -299,37 +185,28 @@ extern "C" int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_
     return fail(F3D_E_UNSUPPORTED, msg);
   }
 
-  std::lock_guard<std::mutex> lock(g_mtx);
   unsigned char* base = nullptr;
   int rc = scratch_on_current_device(&base);
   if (rc != F3D_OK) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t ce = cudaSuccess;
 
-  // Tables on the host (stack and static storage only), then one upload into
-  // the head of the scratch array: [win_ana | syn_a | syn_b | pattern | sharpen | gs].
+  // Tables on the host (stack storage only), then into the head of the
+  // scratch array through the parameters of the table kernel.
   Twiddles tw{};
-  twiddles_into(ip.bw, tw.row);
-  twiddles_into(ip.bh, tw.col);
-  float* h_ana = g_host.win;
-  float* h_sa = h_ana + bwbh;
-  float* h_sb = h_sa + bwbh;
-  float* h_pat = h_sb + bwbh;
-  float* h_shp = h_pat + ps;
-  float* h_gs = h_shp + ps;
-  if (ip.mode == 0) {
-    window_mode0_into(ip.bw, ip.bh, h_ana);
-  } else {
-    windows_mode1_into(ip.bw, ip.bh, ip.ow, ip.oh, ip.wintype, h_ana, h_sa, h_sb);
-  }
-  if (ip.use_pattern) pattern_into(ip.bw, ip.bh, ip.bt, ip.sigma * 255.0f, ip.sigma2, ip.sigma3, ip.sigma4, h_pat);
-  if (ip.sharpen_on) sharpen_into(ip.bw, ip.bh, ip.sharpen, ip.svr, ip.scutoff, h_shp);
-  if (ip.degrid_on) degrid_into(ip.bw, ip.bh, ip.degrid, h_ana, tw.row, tw.col, h_gs);
-  // The staging lives in g_host, contiguous from h_ana; pageable copies return
-  // once the bytes are staged, so the next call may rewrite g_host.
-  cudaError_t ce = cudaMemcpyAsync(base, h_ana, tab_floats * sizeof(float), cudaMemcpyHostToDevice, st);
-  if (ce != cudaSuccess) {
-    cudaGetLastError();
-    return fail(F3D_E_CUDA, "FFT3DCL: table upload into the no-alloc scratch failed");
+  twiddles_into(ip.bw, reinterpret_cast<float*>(tw.row));
+  twiddles_into(ip.bh, reinterpret_cast<float*>(tw.col));
+  float tabs[kMaxTabFloats];
+  build_tables_into(ip, reinterpret_cast<const float*>(tw.row), reinterpret_cast<const float*>(tw.col), tabs);
+  for (size_t off = 0; off < tab_floats; off += kPieceFloats) {
+    TablePiece piece;
+    piece.dst = reinterpret_cast<float*>(base) + off;
+    piece.n = (int)(tab_floats - off < (size_t)kPieceFloats ? tab_floats - off : (size_t)kPieceFloats);
+    std::memcpy(piece.v, tabs + off, sizeof(float) * piece.n);
+    k_noalloc_tables<<<8, 256, 0, st>>>(piece);
+    count_launch();
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) return fail(F3D_E_CUDA, "FFT3DCL: table launch of the no-alloc call failed");
   }
   float* d_ana = reinterpret_cast<float*>(base);
   float* d_sa = d_ana + bwbh;

@@ -217,10 +217,10 @@ size_t f3d_live_bytes(void);
 uint64_t f3d_kernel_launches(void);
 
 /* Denoise one frame without allocating device memory. No counterpart in the
- * reference: it exists for callers that cannot call cudaMalloc -- code that
- * runs while a CUDA graph is being captured, hosts that hand out a fixed
- * device-memory budget up front, and real-time threads that must not take
- * cudaMalloc/cudaFree's device-wide synchronisation.
+ * reference: it exists for callers that cannot call cudaMalloc -- hosts that
+ * hand out a fixed device-memory budget up front and own every byte of it,
+ * and real-time threads that must not take cudaMalloc/cudaFree's device-wide
+ * synchronisation.
  *
  * The caller passes the window frames (`nwin` device pointers in temporal
  * order, bt of them for bt >= 2, else one; rows `src_pitch` bytes apart) and
@@ -229,16 +229,21 @@ uint64_t f3d_kernel_launches(void);
  * the result has the same bits as f3d_forward_device + f3d_process_device.
  * Spectra, windowed blocks and tables live in one static device array of
  * F3D_NOALLOC_SCRATCH_BYTES that every GPU that loads this library holds
- * until the process exits. The first call on a device looks the array's
- * address up (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture. All calls share the array and it keeps the
- * last call's contents; every byte a call reads is written by that call
- * first. Calls whose work overlaps on a GPU race on the array: order them
- * (one stream, or events). Kalman (bt=0) needs state across frames and is
- * refused, as is any plane whose spectra and blocks do not fit the array
- * (F3D_E_UNSUPPORTED, message says how many bytes it needs). Calls no
- * cudaMalloc, cudaFree or other allocating routine; host memory is not
- * allocated either. */
+ * until the process exits. The first call on a device (and the first after a
+ * cudaDeviceReset) looks the array's address up with cudaGetSymbolAddress,
+ * that device current; make that first call before any stream capture. All
+ * calls share the array and it keeps the last call's contents; every byte a
+ * call reads is written by that call first, on its stream. Calls whose work
+ * overlaps on a GPU race on the array: order them (one stream, or events).
+ * Kalman (bt=0) needs state across frames and is refused, as are blocks above
+ * 64 and any plane whose spectra and blocks do not fit the array
+ * (F3D_E_UNSUPPORTED, the message says how many bytes it needs). What fits:
+ * tables + nwin * round256(8 * nblocks * (bw/2+1) * bh) +
+ * round256(4 * nblocks * bw * bh) bytes <= 64 MiB: with 32x32 blocks at
+ * half overlap up to about 0.6 M samples at bt=4 (1024x576 fits, 1280x720
+ * does not) and about 0.9 M at bt=3 (1280x720 fits). Calls no
+ * cudaMalloc, cudaFree or other allocating routine and allocate no host
+ * memory; the tables are built in about 110 KB of the calling thread's stack. */
 #define F3D_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
 int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
                         const void* const* dev_window, int nwin, size_t src_pitch, void* dev_dst,

@@ -1,8 +1,8 @@
 """f3d_denoise_noalloc: the entry point for callers that cannot call
-cudaMalloc (code running during CUDA-graph capture, hosts with a fixed
-device-memory budget, real-time threads that must not take cudaMalloc's
-device-wide synchronisation). Its spectra, windowed blocks and tables live in
-one static device array shared by every call.
+cudaMalloc (hosts that hand out a fixed device-memory budget up front,
+real-time threads that must not take cudaMalloc's device-wide
+synchronisation). Its spectra, windowed blocks and tables live in one static
+device array shared by every call.
 
 Checked through the C ABI against the engine's own entry points
 (f3d_forward_raw + f3d_process_raw) with the exact form's tolerance -- bit
@@ -90,12 +90,28 @@ def test_noalloc_equals_engine_on_calls_in_a_row():
     assert free1 >= free0 - (4 << 20)  # torch's own small input buffers at most
 
 
+def test_noalloc_size_limit():
+    # 1024x576 at bt=4 with 32x32 blocks needs 53,953,024 bytes of the
+    # 64 MiB array; 1280x720 needs 81,134,080 and is refused.
+    frames = synth.moving_rects(1024, 576, 4, 31, lo=16, hi=235, noise=3.0)
+    rc, got = call_noalloc(frames, 8, bt=4)
+    assert rc == F.F3D_OK, F.lib().f3d_last_error().decode()
+    np.testing.assert_array_equal(got, engine_output(frames, 8, bt=4))
+    over = [np.zeros((720, 1280), np.uint8) for _ in range(4)]
+    rc, _ = call_noalloc(over, 8, bt=4)
+    assert rc == -5  # F3D_E_UNSUPPORTED
+    msg = F.lib().f3d_last_error().decode()
+    assert "81134080 bytes" in msg and "no-alloc limit" in msg
+
+
 def test_noalloc_rejects_what_it_cannot_hold():
     big = [np.zeros((2160, 3840), np.uint16) for _ in range(4)]
     rc, _ = call_noalloc(big, 10, bt=4)
     assert rc == -5  # F3D_E_UNSUPPORTED
     msg = F.lib().f3d_last_error().decode()
     assert "no-alloc limit" in msg and "bytes" in msg
+    rc, _ = call_noalloc(synth.clip_gray8(frames=1), 8, bt=1, bw=128, bh=128)
+    assert rc == -5 and "4..64" in F.lib().f3d_last_error().decode()
     rc, _ = call_noalloc(synth.clip_gray8(frames=1), 8, bt=0)
     assert rc == -5 and "Kalman" in F.lib().f3d_last_error().decode()
     rc, _ = call_noalloc(synth.clip_gray8(frames=2), 8, bt=3)
