@@ -56,6 +56,13 @@ NCU_TRAFFIC_BATCH = {4: 1002927925 + 479516689, 8: 1581975962 + 1102231724, 10: 
 DEFAULT_OUTPUTS_PER_STEP = 10
 
 
+# Arithmetic of each form's block transforms: the tensor-core form contracts
+# fp16 hi/lo operand parts (hi*hi + hi*lo + lo*hi) with fp32 accumulation;
+# the filter and everything outside the contractions is fp32.
+DTYPE_OF_FORM = {"exact": "f32", "fast": "f32",
+                 "tc": "f16 hi/lo split operands (3 products), f32 accumulate; f32 filter"}
+
+
 def algorithmic_bytes(nb: int, fbw: int, bh: int, bt: int) -> dict:
     """Bytes one output frame must move with resident spectra: the raw plane
     in, the packed plane out, the new frame's spectrum written once and the
@@ -577,7 +584,7 @@ def run_gpu(args, rank, world, local_rank):
     line = {
         "metric": METRIC, "value": round(fps, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": DTYPE_OF_FORM[args.form],
         "data": "synthetic (seeded ramp + moving rectangles, Gaussian noise 12 LSB, 10-bit)",
         "config": {"workload": WORKLOAD if kframes == 1 else WORKLOAD.replace(
                        "one output frame per step", f"{kframes} consecutive output frames per step"),

@@ -85,27 +85,32 @@ def _run(cmd):
     return r.stderr
 
 
-def vs_include_dir():
-    """Directory holding VapourSynth4.h and VSHelper4.h, or None.
+VS_HEADERS = ("VapourSynth4.h", "VSHelper4.h")
+VS_CACHE = os.path.join(BUILD, "vsinclude")
 
-    Looked up in $VAPOURSYNTH_INCLUDE, the usual system locations, and
-    _build/vsinclude (a copy taken at build time from a source tree that has
-    the headers, so that a build elsewhere from the same working tree finds
-    them too)."""
-    cands = [os.environ.get("VAPOURSYNTH_INCLUDE", ""), "/usr/include/vapoursynth",
-             "/usr/local/include/vapoursynth", os.path.join(BUILD, "vsinclude")]
-    ref = "/root/reference/third_party/vapoursynth"
-    if os.path.exists(os.path.join(ref, "VapourSynth4.h")):
-        dst = os.path.join(BUILD, "vsinclude")
-        os.makedirs(dst, exist_ok=True)
-        for h in ("VapourSynth4.h", "VSHelper4.h"):
-            if not os.path.exists(os.path.join(dst, h)):
-                shutil.copy(os.path.join(ref, h), os.path.join(dst, h))
-    for c in cands:
-        if c and os.path.exists(os.path.join(c, "VapourSynth4.h")) and \
-                os.path.exists(os.path.join(c, "VSHelper4.h")):
+
+def _has_vs_headers(d: str) -> bool:
+    return bool(d) and all(os.path.exists(os.path.join(d, h)) for h in VS_HEADERS)
+
+
+def vs_include_dir():
+    """Directory holding the VapourSynth API-4 headers (VapourSynth4.h,
+    VSHelper4.h; LGPL, not part of this repository), or None.
+
+    Looked up in $VAPOURSYNTH_INCLUDE, the usual system locations and
+    _build/vsinclude. Headers found elsewhere are copied into _build/vsinclude
+    (git-ignored), so that a build from a copy of this working tree on another
+    machine finds them too."""
+    for c in (os.environ.get("VAPOURSYNTH_INCLUDE", ""), "/usr/include/vapoursynth",
+              "/usr/local/include/vapoursynth"):
+        if _has_vs_headers(c):
+            os.makedirs(VS_CACHE, exist_ok=True)
+            for h in VS_HEADERS:
+                dst = os.path.join(VS_CACHE, h)
+                if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(os.path.join(c, h)):
+                    shutil.copy(os.path.join(c, h), dst)
             return c
-    return None
+    return VS_CACHE if _has_vs_headers(VS_CACHE) else None
 
 
 def build(verbose: bool = False) -> str:
@@ -124,6 +129,9 @@ def build(verbose: bool = False) -> str:
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
     vsinc = vs_include_dir()
     psrc = os.path.join(CSRC, "f3d_plugin.cpp")
+    if not vsinc:
+        print("fft3dcl_gb300.build: VapourSynth API-4 headers not found ($VAPOURSYNTH_INCLUDE); "
+              "the plugin library is not built", file=sys.stderr)
     if vsinc and os.path.exists(psrc):
         pobj = os.path.join(BUILD, "f3d_plugin.o")
         if _stale(pobj, [psrc] + glob.glob(os.path.join(CSRC, "*.hpp"))):

@@ -2,17 +2,12 @@
 identifier, namespace, function name and argument string as the reference
 (src/fft3dcl.cpp:540-552), and its argument errors. Runs where the plugin
 was built, i.e. where the VapourSynth headers were found."""
-import json
-import os
-import subprocess
-
 import pytest
 
 import fft3dcl_gb300 as F
 import oracle
-from fft3dcl_gb300 import build
+import plugin_host
 
-HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ARGS = ("clip:vnode;sigma:float:opt;beta:float:opt;bw:int:opt;bh:int:opt;bt:int:opt;sharpen:float:opt;"
             "plane:int:opt;mode:int:opt;bordersize:int:opt;precision:int:opt;degrid:float:opt;scutoff:float:opt;"
             "svr:float:opt;smin:float:opt;smax:float:opt;kratio:float:opt;ow:int:opt;oh:int:opt;wintype:int:opt;"
@@ -21,15 +16,9 @@ REF_ARGS = ("clip:vnode;sigma:float:opt;beta:float:opt;bw:int:opt;bh:int:opt;bt:
 
 @pytest.fixture(scope="module")
 def results(tmp_path_factory):
-    vsinc = build.vs_include_dir()
-    if not vsinc or not os.path.exists(build.PLUGIN):
+    if not plugin_host.plugin_available():
         pytest.skip("plugin not built here (no VapourSynth headers)")
-    exe = str(tmp_path_factory.mktemp("vsmock") / "mock_host")
-    subprocess.run(["g++", "-std=c++17", "-O1", "-I", vsinc, os.path.join(HERE, "vsmock", "mock_host.cpp"),
-                    "-o", exe, "-ldl"], check=True)
-    out = subprocess.run([exe, build.PLUGIN], capture_output=True, text=True, timeout=120)
-    assert out.returncode == 0, out.stderr
-    return {d["case"]: d for d in (json.loads(line) for line in out.stdout.splitlines() if line.strip())}
+    return plugin_host.run_cases(plugin_host.compile_host(str(tmp_path_factory.mktemp("vsmock"))))
 
 
 def test_registration_matches_reference(results):
