@@ -133,25 +133,41 @@ __device__ __forceinline__ float block_dc(const InvArgs& a, int b) {
   return a.dg ? a.s[a.cur][(size_t)b * a.g.bh * a.g.fbw].x : 0.0f;
 }
 
+// The per-bin table values of bin i (0 <= i < bh*fbw): degrid sample, sigma
+// pattern and sharpen factor, read only where they are on. Kernels that
+// filter the same bin of several blocks read them once.
+struct BinTables {
+  float2 gs;
+  float pat, shp;
+};
+__device__ __forceinline__ BinTables bin_tables(const InvArgs& a, int i) {
+  BinTables t{make_float2(0.0f, 0.0f), 0.0f, 0.0f};
+  if (a.dg) t.gs = a.gs[i];
+  if (a.pat) t.pat = a.pattern[i];
+  if (a.shp) t.shp = a.sharpen[i];
+  return t;
+}
+
 // Temporal filter + sharpen of bin i (0 <= i < bh*fbw) of a block whose
-// current-frame DC is dc, with gi = b*bh*fbw + i and sv the bin's window
-// spectra (load_window). Follows
+// current-frame DC is dc, with tb the bin's tables (bin_tables(a, i)),
+// gi = b*bh*fbw + i and sv the bin's window spectra (load_window). Follows
 // src/cpu/reference.cpp:229-409 per bin: degrid correction, bm 2/3/4
 // temporal DFT + Wiener, bm 1 Wiener, bm 0 Kalman (state updated in place),
 // bm -1 pass-through, then sharpen. FAST evaluates the 3- and 4-point
 // temporal transforms with fewer additions (a different rounding; the exact
 // form keeps the reference's expressions).
 template <int BM, bool FAST = false>
-__device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i, size_t gi, const float2 (&sv)[4]) {
+__device__ __forceinline__ float2 filter_vals_t(const InvArgs& a, float dc, const BinTables& tb, size_t gi,
+                                                const float2 (&sv)[4]) {
   float d_re = 0.0f, d_im = 0.0f;
   if (a.dg) {
-    const float2 g = a.gs[i];
+    const float2 g = tb.gs;
     d_re = dc * g.x;
     d_im = dc * g.y;
   }
   float sx = a.sigma_x, sy = a.sigma_y;
   if (a.pat) {
-    const float pv = a.pattern[i];
+    const float pv = tb.pat;
     sx = pv * a.beta;
     sy = pv;
   }
@@ -281,7 +297,7 @@ __device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i,
     fi = im;
   } else if (bm == 0) {
     const float2 c = sv[0];
-    const float cn = a.pat ? a.pattern[i] : a.kalman_cn;
+    const float cn = a.pat ? tb.pat : a.kalman_cn;
     float2 l;
     float s;
     if (a.kalman_init) {  // src/cpu/reference.cpp:336-355: last = current, covar = proc = cn
@@ -322,7 +338,7 @@ __device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i,
       im -= d_im;
     }
     float psd = re * re + im * im + 0.0000000000000000000000000000000000001f;
-    float factor = a.sharpen[i];
+    float factor = tb.shp;
     float g = 1.0f + factor * sqrtf(psd * a.ssmax / ((psd + a.ssmin) * (psd + a.ssmax)));
     re *= g;
     im *= g;
@@ -334,6 +350,11 @@ __device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i,
     fi = im;
   }
   return make_float2(fr, fi);
+}
+
+template <int BM, bool FAST = false>
+__device__ __forceinline__ float2 filter_vals(const InvArgs& a, float dc, int i, size_t gi, const float2 (&sv)[4]) {
+  return filter_vals_t<BM, FAST>(a, dc, bin_tables(a, i), gi, sv);
 }
 
 // The window's spectra of bin gi, in temporal order (frames the mode reads).

@@ -77,9 +77,10 @@ struct TcCfg {
 };
 
 constexpr int kTcThreads = 256;
-// Filter-kernel variants: CTAs per SM and the bins whose loads are in flight
-// together; fewer CTAs leave registers for deeper batches.
-__host__ __device__ constexpr int filter_batch(int minb) { return minb >= 5 ? 1 : (minb == 4 ? 2 : 4); }
+// Filter-kernel variants: CTAs per SM (minb) and filter_batch(minb), the
+// blocks of a group whose spectra loads are in flight together; fewer CTAs
+// leave registers for deeper batches.
+__host__ __device__ constexpr int filter_batch(int minb) { return minb >= 5 ? 1 : 2; }
 constexpr uint64_t kWaitNs = 1000000000ull;  // one second
 
 // ---- forward ---------------------------------------------------------------
@@ -612,9 +613,6 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   const bool last_strip = strip == sa.strips - 1;
   const int own = last_strip ? C::G : C::G - 1;
   const int nvbin = max(0, min(own, min(sa.cells_x + 1, ncols) - J0)) * C::PS;  // bins filtered here
-  constexpr int NBIN = C::G * C::PS;
-  constexpr int NB = NBIN / kTcThreads;
-  static_assert(NBIN % kTcThreads == 0, "bins per thread");
   constexpr int NF = BM >= 2 ? BM : 1;  // window frames read
 
   const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
@@ -634,34 +632,60 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
   }
   __syncthreads();
 
-  // F. Bins tid + 256 j; the loads of kTcFilterBatch bins are issued together.
-  static_assert(kTcFilterBatch >= 1, "batch");
-  // This thread's first bin in each window frame; bin j is kTcThreads * j
-  // further (constant offsets).
-  const float2* sp[NF];
+  // F. Thread t filters bin li = t + 256 r (r < NL) of every block of the
+  // group, the bin's tables read once for all blocks, then tail item q: bin
+  // NL * 256 + e % TAIL of block e / TAIL, e = t + 256 q. The spectra loads of
+  // kTcFilterBatch blocks are issued together; every index is the thread's
+  // base plus a constant.
+  constexpr int NL = C::PS / kTcThreads;
+  constexpr int TAIL = C::PS - NL * kTcThreads;
+  constexpr int NT = TAIL * C::G / kTcThreads;
+  static_assert((TAIL * C::G) % kTcThreads == 0, "tail bins per thread");
+  static_assert(C::G % kTcFilterBatch == 0, "load batches");
+  const int nvb = nvbin / C::PS;  // blocks filtered here
+  const size_t gt = gb0 + tid;
+  if constexpr (NL > 0) {
+    BinTables tb[NL];
 #pragma unroll
-  for (int k = 0; k < NF; k++) sp[k] = a.s[k];
-  const size_t b0i = gb0 + tid;
+    for (int r = 0; r < NL; r++) tb[r] = bin_tables(a, tid + kTcThreads * r);
 #pragma unroll
-  for (int j0 = 0; j0 < NB; j0 += kTcFilterBatch) {
-    float2 sv[kTcFilterBatch][4];
+    for (int b0 = 0; b0 < C::G; b0 += kTcFilterBatch) {
+      float2 sv[kTcFilterBatch][NL][4];
 #pragma unroll
-    for (int u = 0; u < kTcFilterBatch; u++) {
-      const int i = tid + kTcThreads * (j0 + u);
-      if (j0 + u < NB && i < nvbin) {
+      for (int u = 0; u < kTcFilterBatch; u++) {
+        if (b0 + u >= nvb) continue;
 #pragma unroll
-        for (int k = 0; k < NF; k++) sv[u][k] = spec_at<HALF>(sp[k], b0i + kTcThreads * (j0 + u));
+        for (int r = 0; r < NL; r++)
+#pragma unroll
+          for (int k = 0; k < NF; k++)
+            sv[u][r][k] = spec_at<HALF>(a.s[k], gt + (size_t)(b0 + u) * C::PS + kTcThreads * r);
+      }
+#pragma unroll
+      for (int u = 0; u < kTcFilterBatch; u++) {
+        const int b = b0 + u;
+        const float dc = dcs[b];
+#pragma unroll
+        for (int r = 0; r < NL; r++) {
+          const int li = tid + kTcThreads * r;
+          float2 f = make_float2(0.0f, 0.0f);
+          if (b < nvb) f = filter_vals_t<BM, true>(a, dc, tb[r], gb0 + (size_t)b * C::PS + li, sv[u][r]);
+          fbuf[b * S::FS + li] = f;
+        }
       }
     }
+  }
 #pragma unroll
-    for (int u = 0; u < kTcFilterBatch; u++) {
-      if (j0 + u >= NB) continue;
-      const int i = tid + kTcThreads * (j0 + u);
-      const int bl = i / C::PS, li = i - bl * C::PS;
-      float2 f = make_float2(0.0f, 0.0f);
-      if (i < nvbin) f = filter_vals<BM, true>(a, dcs[bl], li, gb0 + i, sv[u]);
-      fbuf[bl * S::FS + li] = f;
+  for (int q = 0; q < NT; q++) {
+    const int e = tid + kTcThreads * q;
+    const int b = e / TAIL, li = NL * kTcThreads + e % TAIL;
+    float2 f = make_float2(0.0f, 0.0f);
+    if (b < nvb) {
+      float2 sv[4];
+#pragma unroll
+      for (int k = 0; k < NF; k++) sv[k] = spec_at<HALF>(a.s[k], gb0 + (size_t)b * C::PS + li);
+      f = filter_vals_t<BM, true>(a, dcs[b], bin_tables(a, li), gb0 + (size_t)b * C::PS + li, sv);
     }
+    fbuf[b * S::FS + li] = f;
   }
   __syncthreads();
 

@@ -184,7 +184,7 @@ struct SweepBatch {
 // Launch shape of the tensor-core kernels, picked by the autotuner.
 struct TcTune {
   int fwd_ctas_per_sm = 3;  // persistent forward grid: CTAs per SM (1 to 3; 2 at most with the split)
-  int filter_minb = 5;      // filter kernel variant: 5, 4 or 3 CTAs per SM (load batch 1, 2, 4 bins)
+  int filter_minb = 5;      // filter kernel variant: 5, 4 or 3 CTAs per SM (spectra loads of 1, 2, 2 blocks in flight)
 };
 cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st);
 cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
