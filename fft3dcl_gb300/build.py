@@ -53,7 +53,7 @@ def _units():
         obj = os.path.join(BUILD, f"f3d_k_exact_bw{bw}.o")
         units.append((obj, [NVCC] + NVCC_COMMON + NVCC_EXACT + [f"-DF3D_BW={bw}", "-c", src, "-o", obj],
                        [src] + headers))
-    for name, extra in (("f3d_k_common.cu", NVCC_EXACT), ("f3d_k_fast.cu", NVCC_FAST),
+    for name, extra in (("f3d_k_common.cu", NVCC_EXACT), ("f3d_k_big.cu", NVCC_EXACT), ("f3d_k_fast.cu", NVCC_FAST),
                         ("f3d_k_sweep.cu", NVCC_FAST), ("f3d_k_tc.cu", NVCC_FAST + ["-Xcompiler", "-ffp-contract=off"]),
                         ("f3d_noalloc.cu", NVCC_EXACT + ["-Xcompiler", "-ffp-contract=off"])):
         src = os.path.join(CSRC, name)

@@ -84,6 +84,9 @@ struct f3d_engine {
   uint8_t* d_in = nullptr;   // raw or float plane, width*height*4 bytes
   uint8_t* d_out = nullptr;  // packed or float output plane
   float* d_blocks = nullptr; // nb x bh x bw windowed blocks
+  float2* d_twr = nullptr;   // blocks above 64: device twiddles (bw/2, bh/2 entries)
+  float2* d_twc = nullptr;
+  float2* d_work = nullptr;  // blocks above 64: nb x bh x bw complex inverse work space
   float2* d_klast = nullptr;
   float* d_kcov = nullptr;
   float* d_kproc = nullptr;
@@ -156,8 +159,10 @@ Geo make_geo(const f3d_engine* e) {
 
 Twiddles make_twiddles(const f3d_engine* e) {
   Twiddles t{};
-  for (int k = 0; k < e->ip.bw / 2; k++) t.row[k] = make_float2(e->tw_row[2 * k], e->tw_row[2 * k + 1]);
-  for (int k = 0; k < e->ip.bh / 2; k++) t.col[k] = make_float2(e->tw_col[2 * k], e->tw_col[2 * k + 1]);
+  if (e->ip.bw <= 64)
+    for (int k = 0; k < e->ip.bw / 2; k++) t.row[k] = make_float2(e->tw_row[2 * k], e->tw_row[2 * k + 1]);
+  if (e->ip.bh <= 64)
+    for (int k = 0; k < e->ip.bh / 2; k++) t.col[k] = make_float2(e->tw_col[2 * k], e->tw_col[2 * k + 1]);
   return t;
 }
 
@@ -221,6 +226,8 @@ int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int
   a.chroma_norm = e->cnorm;
   a.win = e->d_win_ana;
   a.spec = spec;
+  a.twr = e->d_twr;
+  a.twc = e->d_twc;
   cudaEventRecord(e->ev[0], e->stream);
   cudaError_t ce;
   if (e->form == F3D_FORM_TC) {
@@ -278,6 +285,9 @@ int inverse_args(f3d_engine* e, const int* window, int n, InvArgs& a) {
   a.ssmax = e->ip.ssmax;
   a.kalman_cn = e->ip.kalman_cn;
   a.kr2 = e->ip.kratio * e->ip.kratio;
+  a.twr = e->d_twr;
+  a.twc = e->d_twc;
+  a.work = e->d_work;
   return F3D_OK;
 }
 
@@ -409,7 +419,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
   if (!form_supported(form, ip.bw, ip.bh))
     return fail_thread(F3D_E_UNSUPPORTED,
                        "FFT3DCL: block size " + std::to_string(ip.bw) + "x" + std::to_string(ip.bh) +
-                           " is not supported by this GPU form (powers of two 4..64)");
+                           " is not supported by this GPU form (powers of two 4..512)");
   int ndev = 0;
   cudaError_t ce = cudaGetDeviceCount(&ndev);
   if (ce != cudaSuccess || ndev <= 0) {
@@ -542,6 +552,13 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
   // The windowed-block buffer of the separate inverse and overlap-add kernels.
   if (!e->fused && (ce = e->alloc(&e->d_blocks, sizeof(float) * bwbh * e->grid.nb)) != cudaSuccess)
     return finish_fail(e->cuda_fail(ce, "buffer allocation"));
+  // Blocks above 64: twiddles in device memory and the inverse's work space.
+  if (big_block(ip.bw, ip.bh)) {
+    if ((ce = up(reinterpret_cast<float**>(&e->d_twr), e->tw_row)) != cudaSuccess ||
+        (ce = up(reinterpret_cast<float**>(&e->d_twc), e->tw_col)) != cudaSuccess ||
+        (ce = e->alloc(&e->d_work, sizeof(float2) * bwbh * e->grid.nb)) != cudaSuccess)
+      return finish_fail(e->cuda_fail(ce, "large-block buffer allocation"));
+  }
   *out = e;
   return F3D_OK;
 }
@@ -568,6 +585,9 @@ void f3d_engine_destroy(f3d_engine* e) {
     e->release(e->d_in, plane_bytes);
     e->release(e->d_out, plane_bytes);
     e->release(e->d_blocks, sizeof(float) * (size_t)e->ip.bw * e->ip.bh * e->grid.nb);
+    e->release(e->d_twr, e->tw_row.size() * sizeof(float));
+    e->release(e->d_twc, e->tw_col.size() * sizeof(float));
+    e->release(e->d_work, sizeof(float2) * (size_t)e->ip.bw * e->ip.bh * e->grid.nb);
     const size_t nbin = (size_t)e->grid.nb * e->ps;
     e->release(e->d_klast, sizeof(float2) * nbin);
     e->release(e->d_kcov, sizeof(float) * nbin);

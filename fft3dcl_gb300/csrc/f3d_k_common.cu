@@ -72,7 +72,7 @@ cudaError_t launch_ola(const OlaArgs& a, cudaStream_t st) {
 static bool pow2_in(int v, int lo, int hi) { return v >= lo && v <= hi && (v & (v - 1)) == 0; }
 
 bool form_supported(int form, int bw, int bh) {
-  if (form == F3D_FORM_EXACT) return pow2_in(bw, 4, 64) && pow2_in(bh, 4, 64);
+  if (form == F3D_FORM_EXACT) return pow2_in(bw, 4, 512) && pow2_in(bh, 4, 512);
   if (form == F3D_FORM_FAST) return pow2_in(bw, 8, 64) && pow2_in(bh, 8, 64);
   if (form == F3D_FORM_TC) return bw == 32 && bh == 32;
   return false;
@@ -81,6 +81,7 @@ bool form_supported(int form, int bw, int bh) {
 cudaError_t launch_forward(int form, const FwdArgs& a, cudaStream_t st) {
   if (form == F3D_FORM_FAST) return launch_forward_fast(a, st);
   if (form != F3D_FORM_EXACT) return cudaErrorNotSupported;
+  if (big_block(a.g.bw, a.g.bh)) return launch_forward_big(a, st);
   switch (a.g.bw) {
   case 4: return launch_forward_exact_bw4(a, st);
   case 8: return launch_forward_exact_bw8(a, st);
@@ -94,6 +95,7 @@ cudaError_t launch_forward(int form, const FwdArgs& a, cudaStream_t st) {
 cudaError_t launch_filter_inverse(int form, const InvArgs& a, cudaStream_t st) {
   if (form == F3D_FORM_FAST) return launch_inverse_fast(a, st);
   if (form != F3D_FORM_EXACT) return cudaErrorNotSupported;
+  if (big_block(a.g.bw, a.g.bh)) return launch_inverse_big(a, st);
   switch (a.g.bw) {
   case 4: return launch_inverse_exact_bw4(a, st);
   case 8: return launch_inverse_exact_bw8(a, st);

@@ -24,7 +24,8 @@ struct Geo {
 enum Fmt : int { FMT_F32 = 0, FMT_U8 = 8, FMT_U16 = 16 };
 
 // FFT twiddles of the reference plans (double -> float), N/2 entries each,
-// for the row (bw) and column (bh) lengths.
+// for the row (bw) and column (bh) lengths up to 64 (larger blocks read them
+// from device tables, FwdArgs/InvArgs::twr, twc).
 struct Twiddles {
   float2 row[32];
   float2 col[32];
@@ -40,6 +41,8 @@ struct FwdArgs {
   float chroma_norm;   // subtracted before windowing (mode-1 chroma)
   const float* win;    // analysis window, bw*bh
   float2* spec;        // out: nb x bh x fbw half spectra
+  const float2* twr;   // blocks above 64: device twiddles, bw/2 and bh/2 entries
+  const float2* twc;
 };
 
 struct InvArgs {
@@ -61,6 +64,9 @@ struct InvArgs {
   const float* win_b;  // synthesis window of odd-parity blocks
   float* blocks;       // out: nb x bh x bw windowed blocks
   float sigma_x, sigma_y, beta_x, beta, ssmin, ssmax, kalman_cn, kr2;
+  const float2* twr;   // blocks above 64: device twiddles, bw/2 and bh/2 entries,
+  const float2* twc;   //   and nb x bh x bw complex work space
+  float2* work;
 };
 
 struct OlaArgs {
@@ -123,6 +129,12 @@ F3D_DECLARE_EXACT(16)
 F3D_DECLARE_EXACT(32)
 F3D_DECLARE_EXACT(64)
 #undef F3D_DECLARE_EXACT
+
+// Exact form for blocks above 64 (f3d_k_big.cu): one CTA per block,
+// transforms through global memory.
+bool big_block(int bw, int bh);
+cudaError_t launch_forward_big(const FwdArgs& a, cudaStream_t st);
+cudaError_t launch_inverse_big(const InvArgs& a, cudaStream_t st);
 
 // Fast-form launchers (f3d_k_fast.cu).
 cudaError_t launch_forward_fast(const FwdArgs& a, cudaStream_t st);

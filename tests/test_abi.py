@@ -125,10 +125,15 @@ def test_engine_fails_loudly_without_gpu():
     assert F.live_bytes() == 0
 
 
-def test_block_size_limit_rejected_before_device_use():
-    # The reference GPU path stops at 64x64 blocks (src/cl/gpu.cpp:82-89).
-    with pytest.raises(F.F3DError, match="not supported"):
-        F.Engine(640, 480, 8, bw=128, bh=128)
+def test_large_blocks_validate_like_the_reference():
+    # Block sizes round up to powers of two and clamp to 512, as the
+    # reference CPU backend does (src/params.h:62-72); the engine takes them
+    # all (its OpenCL backend stopped at 64, src/cl/gpu.cpp:82-89).
+    for bw, want in ((100, 128), (256, 256), (300, 512), (1000, 512)):
+        ip = F.validate(1280, 720, 8, bw=bw, bh=bw)
+        ref = oracle.validate(oracle.script_params(bw=bw, bh=bw), 1280, 720, 8)
+        assert ip.bw == ip.bh == want == ref.bw == ref.bh
+        assert (ip.nx, ip.ny, ip.ow, ip.oh) == (ref.nx, ref.ny, ref.ow, ref.oh)
 
 
 def test_plane_selection_errors():

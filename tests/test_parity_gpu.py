@@ -86,6 +86,52 @@ def test_block_sizes_and_modes_exact(bw, bh, bt, extra):
         np.testing.assert_array_equal(g, r)
 
 
+# Blocks above 64, up to the reference CPU backend's 512 (src/params.h:62-72):
+# the exact form's large-block kernels (one CTA per block, transforms through
+# global memory), in every temporal mode, mode 0, general overlap, 16-bit and
+# float samples; every form asked for runs them.
+BIG = [
+    (128, 128, 3, {}, 8, "exact"), (256, 64, 2, {"sharpen": 0.3}, 8, "fast"),
+    (512, 512, 1, {}, 8, "tc"), (128, 32, 0, {"sigma2": 3.0}, 8, "exact"),
+    (16, 256, 4, {"mode": 0}, 8, "exact"), (128, 128, 4, {"ow": 48, "oh": 40}, 8, "exact"),
+    (256, 256, -1, {"sharpen": 0.4}, 8, "exact"), (128, 64, 3, {"wintype": 2, "degrid": 0.6}, 12, "exact"),
+    (64, 128, 2, {"wintype": 1}, 32, "fast"),
+]
+
+
+@pytest.mark.parametrize("bw,bh,bt,extra,bits,form", BIG,
+                         ids=[f"{c[0]}x{c[1]}_bt{c[2]}_{c[4]}bit_{c[5]}" for c in BIG])
+def test_large_blocks_exact(bw, bh, bt, extra, bits, form):
+    w, h = (600, 400) if max(bw, bh) >= 256 else (300, 210)
+    seed = bw * 7 + bh + bt
+    if bits == 32:
+        frames = synth.moving_rects(w, h, 5, seed, lo=0.06, hi=0.92, noise=0.01, dtype=np.float32, n_rects=5)
+    elif bits > 8:
+        frames = synth.moving_rects(w, h, 5, seed, lo=200, hi=3900, noise=20.0, dtype=np.uint16,
+                                    maxval=(1 << bits) - 1, n_rects=5)
+    else:
+        frames = synth.moving_rects(w, h, 5, seed, lo=16, hi=235, noise=4.0, n_rects=5)
+    params = dict(bw=bw, bh=bh, bt=bt, **extra)
+    with F.Engine(w, h, bits, 1 if bits == 32 else 0, form=form, **params) as e:
+        assert e.info().form == F.FORMS["exact"]
+    got = gpu_clip(frames, bits, form=form, **params)
+    ref = oracle.run_clip(frames, bits, threads=THREADS, **params)
+    for g, r in zip(got, ref):
+        np.testing.assert_array_equal(g, r)
+    assert F.live_instances() == 0 and F.live_bytes() == 0
+
+
+@pytest.mark.parametrize("bw,bh", [(128, 128), (512, 256), (8, 512)])
+def test_large_block_spectra_exact(bw, bh):
+    rng = np.random.default_rng(bw + bh)
+    plane = rng.integers(0, 256, (230, 301)).astype(np.uint8)
+    with F.Engine(301, 230, 8, bw=bw, bh=bh) as e:
+        e.forward_raw(3, plane)
+        spec = e.spectra(3)
+    pl = oracle.Plane(301, 230, 8, bw=bw, bh=bh)
+    np.testing.assert_array_equal(spec, pl.spectra(pl.upload(plane)))
+
+
 @pytest.mark.parametrize("nframes,bt", [(1, 3), (1, 4), (2, 3), (2, 4), (3, 4), (3, 2), (1, 0)])
 def test_short_clips_clamp_the_window(nframes, bt):
     # Clips of 1-3 frames with bt=3/4: window indices clamp to the clip
