@@ -610,22 +610,52 @@ def run_gpu(args, rank, world, local_rank):
             workload="1920x1080 YUV420P8 all planes, sigma=2.5 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4 scutoff=0.3 "
                      "svr=1 smin=4 smax=20 degrid=1, clip resident in HBM", **yuv_batched(args, dev, local_rank))
     if world == 1 and args.serve_streams > 0:
-        # The serving workload: mixed streams with Poisson frame arrivals,
-        # through the serving loop (continuous batching, HBM-budget admission).
+        # The serving workload: YUV 4:2:0 video streams (all planes) with
+        # Poisson frame arrivals through the serving loop (shared steps for
+        # the tensor-core streams, HBM-budget admission); then the same
+        # streams with the arrival rates scaled up until the delivered rate
+        # falls behind the offered one (saturation).
         from fft3dcl_gb300 import serving
         specs = serving.mixed_streams(args.serve_streams, args.serve_frames)
         sframes = [serving.stream_frames(s, distinct=4) for s in specs]
-        with F.Server(form=args.form, device=local_rank, max_streams=args.serve_streams,
-                      hbm_budget=200 << 30) as sv:
-            _, st = serving.run(sv, specs, sframes, realtime=True, timeout_s=300)
+
+        def serve(rate):
+            with F.Server(form=args.form, device=local_rank, max_streams=3 * len(specs),
+                          hbm_budget=200 << 30) as sv:
+                return serving.run(sv, specs, sframes, realtime=True, rate=rate, timeout_s=300, keep_outputs=False)[1]
+
+        def point(rate, st):
+            return {"rate_x": rate, "offered_frames_per_s": round(st["offered_frames_per_s"], 1),
+                    "frames_per_s": round(st["frames_per_s"], 1), "p50_ms": round(st["p50_ms"], 3),
+                    "p99_ms": round(st["p99_ms"], 3), "server_p99_ms": round(st["server_p99_ms"], 3),
+                    "submit_lag_p99_ms": round(st["submit_lag_p99_ms"], 3),
+                    "shared_steps": st["shared_steps"], "outputs_per_shared_step":
+                        round(st["shared_outputs"] / st["shared_steps"], 2) if st["shared_steps"] else None}
+
+        st = serve(1.0)
+        sweep = [point(1.0, st)]
+        for rate in (2.0, 4.0, 8.0, 16.0, 32.0, 64.0, 128.0):
+            sweep.append(point(rate, serve(rate)))
+            # Saturated: the delivered rate falls behind the offered one, or
+            # frames queue for longer than a tenth of a second.
+            if sweep[-1]["frames_per_s"] < 0.9 * sweep[-1]["offered_frames_per_s"] or sweep[-1]["p99_ms"] > 100.0:
+                break
+        capacity = max(p["frames_per_s"] for p in sweep)
         line["serving"] = {
             "streams": len(specs), "frames_per_stream": args.serve_frames,
             "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3), "max_ms": round(st["max_ms"], 3),
-            "frames_per_s": round(st["frames"] / st["seconds"], 1) if st["seconds"] > 0 else None,
-            "offered_frames_per_s": round(sum(s["fps"] for s in specs), 1),
-            "mix": "resolutions 640x360..3840x2160, 8/10-bit luma, bt in {1,3,4}, bw in {16,32} (bw 16 runs the fast form)",
-            "arrivals": "Poisson, 24-60 frames/s per stream",
-            "latency": "arrival of the last input frame an output's window needs -> output copied to host memory",
+            "server_p50_ms": round(st["server_p50_ms"], 3), "server_p99_ms": round(st["server_p99_ms"], 3),
+            "frames_per_s": round(st["frames_per_s"], 1),
+            "offered_frames_per_s": round(st["offered_frames_per_s"], 1),
+            "shared_steps": st["shared_steps"], "max_outputs_per_shared_step": st["max_shared"],
+            "capacity_frames_per_s": capacity,
+            "load_sweep": sweep,
+            "mix": "YUV420P8/P10 video streams, all three planes (one server stream per plane), resolutions "
+                   "640x360..3840x2160, bt in {1,3,4}, bw in {16,32} (bw 16 runs the fast form on its own "
+                   "CUDA stream; the tensor-core streams share steps)",
+            "arrivals": "Poisson, 24-60 frames/s per stream (rate_x scales every stream's rate)",
+            "latency": "per video frame: scheduled arrival of the last frame its temporal window needs -> last "
+                       "plane's output copied to host memory (server_*: from that frame's arrival at the server)",
             "form": args.form}
     if world == 1 and not args.no_cpu:
         cpu_threads = os.cpu_count() or 1

@@ -99,7 +99,7 @@ EXPORTS = (
     "f3d_process_device", "f3d_prune", "f3d_synchronize", "f3d_last_kernel_ms",
     "f3d_live_instances", "f3d_live_bytes", "f3d_kernel_launches", "f3d_denoise_noalloc",
     "f3d_server_create", "f3d_server_destroy", "f3d_server_open", "f3d_server_submit", "f3d_server_poll",
-    "f3d_server_close", "f3d_server_get_stats",
+    "f3d_server_poll_timed", "f3d_server_close", "f3d_server_get_stats",
     "f3d_batch_create", "f3d_batch_destroy", "f3d_batch_error", "f3d_batch_step", "f3d_batch_tune",
     "f3d_batch_set_tune", "f3d_batch_last_kernel_ms",
 )
@@ -155,6 +155,7 @@ def lib():
         L.f3d_server_open.argtypes = [vp, P(ScriptParams), P(PlaneGeom), i, P(i)]
         L.f3d_server_submit.argtypes = [vp, i, i, vp, C.c_longlong]
         L.f3d_server_poll.argtypes = [vp, i, P(i), vp, C.c_longlong, i]
+        L.f3d_server_poll_timed.argtypes = [vp, i, P(i), vp, C.c_longlong, i, P(C.c_double), P(C.c_double)]
         L.f3d_server_close.argtypes = [vp, i]
         L.f3d_server_get_stats.argtypes = [vp, P(ServerStats)]
         L.f3d_prune.argtypes = [vp, i, i]
@@ -174,7 +175,8 @@ class ServerConfig(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("frames", C.c_longlong), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("max_ms", C.c_double), ("mean_ms", C.c_double), ("seconds", C.c_double),
-                ("open_streams", C.c_int), ("used_bytes", C.c_size_t)]
+                ("open_streams", C.c_int), ("used_bytes", C.c_size_t), ("shared_steps", C.c_longlong),
+                ("shared_outputs", C.c_longlong), ("max_shared", C.c_int)]
 
 
 F3D_E_BUSY = -6
@@ -506,7 +508,9 @@ def FFT3DCL(clip, fmt: VideoFormat | None = None, **params):
 class Server:
     """The serving loop (f3d_server_*): many plane streams of any size, depth
     and parameters on one GPU, admitted by an HBM budget, each keeping its
-    window spectra resident, launched concurrently as their frames arrive."""
+    window spectra resident, launched as their frames arrive: tensor-core
+    streams in shared steps (one launch per kernel for many streams), the
+    others concurrently on their own CUDA streams."""
 
     def __init__(self, form: str = "tc", device: int = 0, max_streams: int = 16,
                  hbm_budget: int = 64 << 30):
@@ -552,6 +556,24 @@ class Server:
                                               out.strides[0], timeout_ms)):
             return None
         return n.value, out
+
+    def poll_timed(self, sid: int, timeout_ms: int = 0, out: np.ndarray | None = None):
+        """(frame number, output plane, ready ms, done ms) of the stream's next
+        finished output, or None: ready is when the last input frame its
+        window needs arrived, done when its copy to host memory finished (one
+        clock for all streams of the server). `out` (optional) receives the
+        plane instead of a new array."""
+        w, h, dtype = self._geom[sid]
+        if out is None:
+            out = np.empty((h, w), dtype)
+        elif out.shape != (h, w) or out.dtype != dtype or not out.flags.c_contiguous:
+            raise ValueError("FFT3DCL: output buffer does not match the stream's plane")
+        n = C.c_int(-1)
+        t0, t1 = C.c_double(0.0), C.c_double(0.0)
+        if not self._rc(lib().f3d_server_poll_timed(self._h, sid, C.byref(n), out.ctypes.data_as(C.c_void_p),
+                                                    out.strides[0], timeout_ms, C.byref(t0), C.byref(t1))):
+            return None
+        return n.value, out, t0.value, t1.value
 
     def close_stream(self, sid: int):
         self._rc(lib().f3d_server_close(self._h, sid))

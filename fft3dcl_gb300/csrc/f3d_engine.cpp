@@ -1132,3 +1132,68 @@ int f3d_batch_set_tune(f3d_batch* b, int fwd_ctas_per_sm, int filter_minb) {
 
 }  // extern "C"
 
+
+// ---- engine steps shared across engines (the serving loop) -----------------
+
+#include "f3d_engine_internal.hpp"
+
+namespace f3d {
+
+bool engine_batchable(const f3d_engine* e) {
+  return e && e->form == F3D_FORM_TC && e->inv_form == F3D_FORM_TC && e->fused;
+}
+
+uint64_t engine_batch_key(const f3d_engine* e) {
+  const f3d_internal_params& p = e->ip;
+  return (uint64_t)p.bw | ((uint64_t)p.bh << 10) | ((uint64_t)p.ow << 20) | ((uint64_t)p.oh << 30) |
+         ((uint64_t)p.wintype << 40) | ((uint64_t)(p.bm + 1) << 42) | ((uint64_t)e->fmt << 46) |
+         ((uint64_t)e->half << 52);
+}
+
+int engines_step(f3d_engine* const* eng, int n, const int* fns, const void* const* src, const size_t* src_pitch,
+                 const int* const* win, const int* nwin, void* const* dst, const size_t* dst_pitch, cudaStream_t st,
+                 std::string* err) {
+  auto bad = [&](int code, const std::string& m) {
+    if (err) *err = m;
+    return code;
+  };
+  if (n < 1 || n > kMaxBatch) return bad(F3D_E_PARAM, "FFT3DCL: a shared step holds 1 to 16 engines");
+  for (int i = 0; i < n; i++) {
+    if (!engine_batchable(eng[i]) || eng[i]->stream != st ||
+        engine_batch_key(eng[i]) != engine_batch_key(eng[0]))
+      return bad(F3D_E_UNSUPPORTED, "FFT3DCL: engines of a shared step run the fused tensor-core form alike");
+    for (int j = 0; j < i; j++)
+      if (eng[j] == eng[i]) return bad(F3D_E_PARAM, "FFT3DCL: an engine appears twice in a shared step");
+  }
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (int i = 0; i < n; i++) locks.emplace_back(eng[i]->mtx);
+  TcFwdArgs fa[kMaxBatch];
+  SweepArgs sa[kMaxBatch];
+  int nf = 0, ns = 0;
+  for (int i = 0; i < n; i++) {
+    f3d_engine* e = eng[i];
+    if (fns[i] < 0 || e->cache.count(fns[i])) continue;
+    if (!src[i] || src_pitch[i] < (size_t)e->geom.width * e->bps)
+      return bad(F3D_E_PARAM, "FFT3DCL: bad source plane in a shared step");
+    float2* spec = spectra_slot(e, fns[i], true);
+    if (!spec) return bad(F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
+    fa[nf++] = tc_forward_args(e, static_cast<const uint8_t*>(src[i]), (long long)src_pitch[i], e->fmt, spec);
+  }
+  for (int i = 0; i < n; i++) {
+    if (nwin[i] <= 0) continue;
+    f3d_engine* e = eng[i];
+    InvArgs a;
+    const int rc = inverse_args(e, win[i], nwin[i], a);
+    if (rc != F3D_OK) return bad(rc, e->err);
+    if (!dst[i] || dst_pitch[i] < (size_t)e->geom.width * e->bps)
+      return bad(F3D_E_PARAM, "FFT3DCL: bad output plane in a shared step");
+    sa[ns++] = sweep_args(e, a, static_cast<uint8_t*>(dst[i]), (long long)dst_pitch[i], e->fmt);
+  }
+  cudaSetDevice(eng[0]->device);
+  cudaError_t ce = nf ? launch_forward_tc_batch(fa, nf, TcTune{}, st) : cudaSuccess;
+  if (ce == cudaSuccess && ns) ce = launch_sweep_tc_batch(sa, ns, TcTune{}, st, nullptr);
+  if (ce != cudaSuccess) return bad(F3D_E_CUDA, std::string("FFT3DCL: shared step launch: ") + cudaGetErrorString(ce));
+  return F3D_OK;
+}
+
+}  // namespace f3d

@@ -13,11 +13,16 @@
 //  - residency: each stream has its own engine, so its temporal-window
 //    spectra (and Kalman state) stay in HBM between frames;
 //  - continuous batching: one scheduler thread launches, on every pass, the
-//    next output of every stream whose window frames have arrived, each
-//    stream on its own CUDA stream, so the kernels of different streams run
-//    concurrently; streams opened while others run join the next pass;
+//    next output of every stream whose window frames have arrived. Streams
+//    that run the fused tensor-core form share one CUDA stream, and the ready
+//    outputs of all of them whose kernels take the same parameters (block
+//    size, overlap, window, temporal mode, sample format) go into one step:
+//    one launch per kernel for up to sixteen planes of any sizes. Other
+//    streams (fast or exact form, Kalman) launch on their own CUDA streams,
+//    concurrently. Streams opened while others run join the next pass;
 //  - latency: an output's latency runs from the arrival of the last input
 //    frame its window needs to the completion of its readback to host memory.
+#include "f3d_engine_internal.hpp"
 #include "fft3d_gb300.h"
 
 #include <cuda_runtime.h>
@@ -56,6 +61,9 @@ int fail(int code, const std::string& msg) {
 
 constexpr int kInSlots = 6;   // submitted frames a stream may hold before they are uploaded
 constexpr int kOutSlots = 3;  // outputs a stream may hold before they are polled
+// Shared steps queued on the GPU at once: one running and one waiting. While
+// they run, the outputs that become ready collect for the next step.
+constexpr int kMaxInflight = 2;
 
 struct InSlot {
   uint8_t* host = nullptr;  // pinned
@@ -77,7 +85,9 @@ struct OutSlot {
 struct Stream {
   int id = -1;
   f3d_engine* eng = nullptr;
-  cudaStream_t cs = nullptr;
+  cudaStream_t cs = nullptr;  // the stream's own CUDA stream, or the server's shared one (batched)
+  bool own_cs = true;
+  bool batched = false;       // launched in shared steps with other streams
   int W = 0, H = 0, bps = 1, nframes = 0, need = 1, cur = 0, bt = 1;
   size_t row_bytes = 0, plane_bytes = 0, est_bytes = 0;
   uint8_t* d_src = nullptr;
@@ -102,14 +112,26 @@ void free_stream(Stream* s) {
   }
   if (s->d_src) cudaFree(s->d_src);
   if (s->d_dst) cudaFree(s->d_dst);
-  if (s->cs) cudaStreamDestroy(s->cs);
+  if (s->cs && s->own_cs) cudaStreamDestroy(s->cs);
   delete s;
+}
+
+// Whether a stream's engine will run the fused tensor-core form (the
+// conditions of its forward and sweep: mode 1, 32x32 blocks, half overlap,
+// not Kalman), so that it is created on the server's shared stream.
+bool predict_batchable(int form, const f3d_internal_params& ip) {
+  return form == F3D_FORM_TC && ip.bm != 0 && ip.mode == 1 && ip.bw == 32 && ip.bh == 32 && ip.ow * 2 == ip.bw &&
+         ip.oh * 2 == ip.bh;
 }
 
 }  // namespace
 
 struct f3d_server {
   f3d_server_config cfg{};
+  cudaStream_t shared = nullptr;  // CUDA stream of the batched streams
+  std::deque<cudaEvent_t> inflight, spare;  // end events of the queued shared steps, unused ones
+  long long steps = 0, step_outputs = 0;
+  int max_step = 0;
   std::mutex mtx;
   std::condition_variable work_cv, done_cv;
   std::map<int, Stream*> streams;
@@ -123,6 +145,8 @@ struct f3d_server {
   void run();
   bool ready(Stream* s, int n, std::vector<int>& win);
   void launch(Stream* s, int n, const std::vector<int>& win);
+  bool launch_shared();
+  void step_group(std::vector<Stream*>& grp);
   void reap(Stream* s);
 };
 
@@ -190,6 +214,129 @@ void f3d_server::reap(Stream* s) {
   }
 }
 
+// One shared step per group of batched streams whose next outputs are ready
+// and whose kernels take the same parameters (at most sixteen streams a
+// step). Returns whether anything was launched.
+bool f3d_server::launch_shared() {
+  while (!inflight.empty() && cudaEventQuery(inflight.front()) == cudaSuccess) {
+    spare.push_back(inflight.front());
+    inflight.pop_front();
+  }
+  if ((int)inflight.size() >= kMaxInflight) return false;
+  std::map<uint64_t, std::vector<Stream*>> groups;
+  std::vector<int> win;
+  for (auto& kv : streams) {
+    Stream* s = kv.second;
+    if (!s->batched || !s->err.empty() || s->next_out >= s->nframes || (int)s->outs.size() >= kOutSlots) continue;
+    if (!ready(s, s->next_out, win)) continue;
+    groups[f3d::engine_batch_key(s->eng)].push_back(s);
+  }
+  bool any = false;
+  for (auto& kv : groups) {
+    std::vector<Stream*>& all = kv.second;
+    for (size_t i = 0; i < all.size(); i += 16) {
+      std::vector<Stream*> grp(all.begin() + i, all.begin() + std::min(all.size(), i + 16));
+      step_group(grp);
+      any = true;
+    }
+  }
+  if (any) {
+    cudaEvent_t ev = nullptr;
+    if (!spare.empty()) {
+      ev = spare.back();
+      spare.pop_back();
+    } else if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      ev = nullptr;
+    }
+    if (ev) {
+      cudaEventRecord(ev, shared);
+      inflight.push_back(ev);
+    }
+  }
+  return any;
+}
+
+// The next output of every stream of grp in shared steps: the window frames
+// not cached yet go up one per stream and step (forward only), the last
+// with the outputs; then each output is copied to its host slot.
+void f3d_server::step_group(std::vector<Stream*>& grp) {
+  const int n = (int)grp.size();
+  std::vector<std::vector<int>> wins(n), missing(n);
+  std::vector<double> t_ready(n, 0.0);
+  size_t rounds = 1;
+  for (int i = 0; i < n; i++) {
+    Stream* s = grp[i];
+    ready(s, s->next_out, wins[i]);
+    for (int fn : wins[i]) {
+      t_ready[i] = std::max(t_ready[i], s->arrive[fn]);
+      if (!f3d_has(s->eng, fn) && std::find(missing[i].begin(), missing[i].end(), fn) == missing[i].end())
+        missing[i].push_back(fn);
+    }
+    rounds = std::max(rounds, missing[i].size());
+  }
+  f3d_engine* eng[16];
+  int fns[16], nwin[16];
+  const void* src[16];
+  void* dst[16];
+  size_t sp[16], dp[16];
+  const int* wp[16];
+  std::string err;
+  int rc = F3D_OK;
+  for (size_t r = 0; r < rounds && rc == F3D_OK; r++) {
+    const bool last = r + 1 == rounds;
+    for (int i = 0; i < n; i++) {
+      Stream* s = grp[i];
+      eng[i] = s->eng;
+      fns[i] = -1;
+      // Entries with fewer missing frames forward theirs in the first rounds.
+      if (r < missing[i].size()) {
+        const int fn = missing[i][r];
+        for (auto& slot : s->in) {
+          if (slot.state != InSlot::FULL || slot.frame != fn) continue;
+          cudaMemcpyAsync(s->d_src, slot.host, s->plane_bytes, cudaMemcpyHostToDevice, shared);
+          slot.state = InSlot::UPLOADED;
+          slot.seq = s->seq;
+          fns[i] = fn;
+          break;
+        }
+      }
+      src[i] = s->d_src;
+      sp[i] = s->row_bytes;
+      wp[i] = wins[i].data();
+      nwin[i] = last ? (int)wins[i].size() : 0;
+      dst[i] = s->d_dst;
+      dp[i] = s->row_bytes;
+    }
+    rc = f3d::engines_step(eng, n, fns, src, sp, wp, nwin, dst, dp, shared, &err);
+  }
+  if (rc == F3D_OK) {
+    steps++;
+    step_outputs += n;
+    max_step = std::max(max_step, n);
+  }
+  for (int i = 0; i < n; i++) {
+    Stream* s = grp[i];
+    const int out_n = s->next_out++;
+    OutSlot* o = nullptr;
+    for (auto& c : s->out_pool)
+      if (!c.busy) {
+        o = &c;
+        break;
+      }
+    if (rc != F3D_OK && s->err.empty()) s->err = err;
+    cudaMemcpyAsync(o->host, s->d_dst, s->plane_bytes, cudaMemcpyDeviceToHost, shared);
+    cudaEventRecord(o->ev, shared);
+    f3d_prune(s->eng, out_n - s->cur - 1, out_n - s->cur + s->bt);
+    o->busy = true;
+    o->done = false;
+    o->frame = out_n;
+    o->seq = s->seq++;
+    o->t_ready = t_ready[i];
+    s->outs.push_back(o);
+  }
+}
+
 void f3d_server::run() {
   cudaSetDevice(cfg.device);
   std::vector<int> win;
@@ -199,6 +346,7 @@ void f3d_server::run() {
     for (auto& kv : streams) {
       Stream* s = kv.second;
       reap(s);
+      if (s->batched) continue;
       // Continuous batching: every stream whose next window is complete
       // gets its output launched in this pass.
       while (s->next_out < s->nframes && (int)s->outs.size() < kOutSlots && ready(s, s->next_out, win)) {
@@ -206,8 +354,11 @@ void f3d_server::run() {
         s->next_out++;
         any = true;
       }
-      for (OutSlot* o : s->outs) pending |= !o->done;
     }
+    // Shared steps of the batched streams, as long as outputs are ready.
+    for (int k = 0; k < kOutSlots && launch_shared(); k++) any = true;
+    for (auto& kv : streams)
+      for (OutSlot* o : kv.second->outs) pending |= !o->done;
     done_cv.notify_all();
     if (!any) {
       // In-flight outputs are polled every 50 us; otherwise sleep until a
@@ -232,6 +383,12 @@ int f3d_server_create(const f3d_server_config* cfg, f3d_server** out) {
   if (cfg->device < 0 || cfg->device >= ndev) return fail(F3D_E_PARAM, "FFT3DCL: device ordinal out of range");
   auto* sv = new f3d_server();
   sv->cfg = *cfg;
+  cudaSetDevice(cfg->device);
+  if (cudaStreamCreateWithFlags(&sv->shared, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete sv;
+    return fail(F3D_E_CUDA, "FFT3DCL: server stream creation failed");
+  }
   sv->worker = std::thread([sv] { sv->run(); });
   *out = sv;
   return F3D_OK;
@@ -244,6 +401,9 @@ void f3d_server_destroy(f3d_server* sv) {
   if (sv->worker.joinable()) sv->worker.join();
   cudaSetDevice(sv->cfg.device);
   for (auto& kv : sv->streams) free_stream(kv.second);
+  for (cudaEvent_t ev : sv->inflight) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : sv->spare) cudaEventDestroy(ev);
+  if (sv->shared) cudaStreamDestroy(sv->shared);
   delete sv;
 }
 
@@ -255,12 +415,20 @@ int f3d_server_open(f3d_server* sv, const f3d_script_params* sp, const f3d_plane
     std::lock_guard<std::mutex> lk(sv->mtx);
     if ((int)sv->streams.size() >= sv->cfg.max_streams) return fail(F3D_E_BUSY, "FFT3DCL: no free stream slot");
   }
-  auto s = std::unique_ptr<Stream, void (*)(Stream*)>(new Stream(), free_stream);
-  if (cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking) != cudaSuccess)
-    return fail(F3D_E_CUDA, "FFT3DCL: stream creation failed");
-  f3d_options o{sv->cfg.device, sv->cfg.form, s->cs, 0};
-  int rc = f3d_engine_create(sp, geom, &o, &s->eng);
+  f3d_internal_params ip{};
+  int rc = f3d_validate_params(sp, geom->width, geom->height, geom->bits, &ip);
   if (rc != F3D_OK) return rc;
+  auto s = std::unique_ptr<Stream, void (*)(Stream*)>(new Stream(), free_stream);
+  if (predict_batchable(sv->cfg.form, ip)) {
+    s->cs = sv->shared;
+    s->own_cs = false;
+  } else if (cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking) != cudaSuccess) {
+    return fail(F3D_E_CUDA, "FFT3DCL: stream creation failed");
+  }
+  f3d_options o{sv->cfg.device, sv->cfg.form, s->cs, 0};
+  rc = f3d_engine_create(sp, geom, &o, &s->eng);
+  if (rc != F3D_OK) return rc;
+  s->batched = !s->own_cs && f3d::engine_batchable(s->eng);
   f3d_engine_info info{};
   f3d_engine_get_info(s->eng, &info);
   s->W = geom->width;
@@ -270,8 +438,6 @@ int f3d_server_open(f3d_server* sv, const f3d_script_params* sp, const f3d_plane
   s->plane_bytes = s->row_bytes * s->H;
   s->nframes = nframes;
   s->arrive.assign(nframes, 0.0);
-  f3d_internal_params ip{};
-  f3d_validate_params(sp, geom->width, geom->height, geom->bits, &ip);
   s->bt = ip.bt;
   s->need = ip.bm >= 2 ? ip.bt : 1;
   s->cur = ip.bm >= 2 ? ip.current : 0;
@@ -338,6 +504,11 @@ int f3d_server_submit(f3d_server* sv, int sid, int n, const void* src, long long
 }
 
 int f3d_server_poll(f3d_server* sv, int sid, int* n, void* dst, long long pitch, int timeout_ms) {
+  return f3d_server_poll_timed(sv, sid, n, dst, pitch, timeout_ms, nullptr, nullptr);
+}
+
+int f3d_server_poll_timed(f3d_server* sv, int sid, int* n, void* dst, long long pitch, int timeout_ms,
+                          double* ready_ms, double* done_ms) {
   if (!sv || !n) return fail(F3D_E_PARAM, "FFT3DCL: null argument");
   std::unique_lock<std::mutex> lk(sv->mtx);
   auto it = sv->streams.find(sid);
@@ -350,6 +521,8 @@ int f3d_server_poll(f3d_server* sv, int sid, int* n, void* dst, long long pitch,
   if (!s->err.empty()) return fail(F3D_E_CUDA, s->err);
   if (dst && pitch < (long long)s->row_bytes) return fail(F3D_E_PARAM, "FFT3DCL: pitch too small");
   *n = o->frame;
+  if (ready_ms) *ready_ms = o->t_ready;
+  if (done_ms) *done_ms = o->t_done;
   // The copy runs without the server lock, so that the scheduler keeps
   // launching meanwhile; the slot stays busy (not reused) until it is done.
   // One thread polls a stream.
@@ -389,6 +562,9 @@ int f3d_server_get_stats(f3d_server* sv, f3d_server_stats* st) {
   st->frames = (long long)v.size();
   st->open_streams = (int)sv->streams.size();
   st->used_bytes = sv->used_bytes;
+  st->shared_steps = sv->steps;
+  st->shared_outputs = sv->step_outputs;
+  st->max_shared = sv->max_step;
   if (v.empty()) return F3D_OK;
   std::sort(v.begin(), v.end());
   auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * (v.size() - 1) + 0.5))]; };

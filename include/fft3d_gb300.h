@@ -300,11 +300,16 @@ int f3d_batch_last_kernel_ms(f3d_batch* b, float* ms);
  * state stay in HBM). Streams are admitted while the device memory of all open
  * streams fits `hbm_budget` and fewer than `max_streams` are open; otherwise
  * f3d_server_open returns F3D_E_BUSY. On every pass the scheduler launches
- * the next output of every stream whose window frames have arrived, each
- * stream on its own CUDA stream, so streams' kernels overlap on the device
- * and streams that open while others run join at once. Latency of an output:
- * from the arrival of the last input frame its window needs to the end of
- * its copy to host memory. */
+ * the next output of every stream whose window frames have arrived. Streams
+ * whose engines run the fused tensor-core form share one CUDA stream, and
+ * their ready outputs go into shared steps: one launch per kernel for up to
+ * sixteen streams whose kernels take the same parameters (block size,
+ * overlap, window, temporal mode, sample format), planes of any size. The
+ * other streams launch on their own CUDA streams, so their kernels overlap
+ * on the device. Streams that open while others run join at once. Latency of
+ * an output: from the arrival of the last input frame its window needs to
+ * the end of its copy to host memory. A video stream of several planes (YUV)
+ * is one server stream per plane. */
 typedef struct {
   int device;
   int form;          /* F3D_FORM_* for every stream (per-stream fallbacks as in create) */
@@ -318,6 +323,9 @@ typedef struct {
   double seconds;    /* first input ready to last output done */
   int open_streams;
   size_t used_bytes; /* admitted device memory */
+  long long shared_steps;   /* steps launched for several streams at once */
+  long long shared_outputs; /* outputs of those steps */
+  int max_shared;           /* most outputs in one shared step */
 } f3d_server_stats;
 
 typedef struct f3d_server f3d_server;
@@ -335,6 +343,12 @@ int f3d_server_submit(f3d_server* sv, int sid, int n, const void* src, long long
  * timeout_ms; *n receives its frame number and dst (if not NULL) its samples.
  * F3D_E_BUSY when none finished in time. One thread polls a given stream. */
 int f3d_server_poll(f3d_server* sv, int sid, int* n, void* dst, long long pitch, int timeout_ms);
+/* The same, with the output's latency interval: *ready_ms when the last
+ * input frame its window needs arrived, *done_ms when its copy to host
+ * memory finished (milliseconds on one steady clock, the same for all
+ * streams of the server; either pointer may be NULL). */
+int f3d_server_poll_timed(f3d_server* sv, int sid, int* n, void* dst, long long pitch, int timeout_ms,
+                          double* ready_ms, double* done_ms);
 /* Releases the stream and its share of the budget. */
 int f3d_server_close(f3d_server* sv, int sid);
 int f3d_server_get_stats(f3d_server* sv, f3d_server_stats* st);
