@@ -79,6 +79,7 @@ class Options(C.Structure):
 
 
 FLAG_UNFUSED, FLAG_PREFETCH_EARLY, FLAG_PREFETCH_LATE, FLAG_HALF_SPECTRA = 1, 2, 4, 8
+FLAG_TEST_WAIT_TIMEOUT = 1 << 20  # tests of the error path only (include/fft3d_gb300.h)
 
 
 class EngineInfo(C.Structure):

@@ -80,6 +80,7 @@ struct f3d_engine {
   std::vector<float2*> pool;
   int pool_min = 2;  // spectra the retire pool keeps whatever the budget: a batch raises it to its outputs per step
   bool half = false; // spectra stored as fp16 pairs (F3D_FLAG_HALF_SPECTRA applied)
+  bool test_skip = false; // F3D_FLAG_TEST_WAIT_TIMEOUT, not applied yet
 
   uint8_t* d_in = nullptr;   // raw or float plane, width*height*4 bytes
   uint8_t* d_out = nullptr;  // packed or float output plane
@@ -312,6 +313,7 @@ SweepArgs sweep_args(const f3d_engine* e, const InvArgs& a, uint8_t* ddst, long 
   sa.tab = e->d_tc;
   sa.err = e->d_err;
   sa.img = e->d_img;
+  sa.test_skip = e->test_skip ? 1 : 0;
   return sa;
 }
 
@@ -322,6 +324,7 @@ int run_process(f3d_engine* e, const int* window, int n, uint8_t* ddst, long lon
   if (e->fused) {
     // One fused launch (plus the seam merge) writes the packed plane.
     const SweepArgs sa = sweep_args(e, a, ddst, pitch, fmt);
+    e->test_skip = false;
     cudaEventRecord(e->ev[2], e->stream);
     cudaError_t ce = e->inv_form == F3D_FORM_TC ? launch_sweep_tc_batch(&sa, 1, e->tune, e->stream, e->ev[4])
                                                 : launch_sweep(e->inv_form, sa, e->stream, e->ev[4]);
@@ -547,6 +550,7 @@ int f3d_engine_create(const f3d_script_params* sp, const f3d_plane_geom* geom,
     // and the tensor-core kernels read and write it.
     e->half = (fl & F3D_FLAG_HALF_SPECTRA) && e->form == F3D_FORM_TC && e->inv_form == F3D_FORM_TC &&
               e->fmt == FMT_U8 && ip.precision < 2;
+    e->test_skip = (fl & F3D_FLAG_TEST_WAIT_TIMEOUT) && e->inv_form == F3D_FORM_TC;
     if (e->half) e->spec_bytes = sizeof(__half2) * (size_t)e->grid.nb * e->ps;
   }
   // The windowed-block buffer of the separate inverse and overlap-add kernels.
@@ -766,7 +770,16 @@ int f3d_synchronize(f3d_engine* e) {
     int flag = 0;
     ce = cudaMemcpy(&flag, e->d_err, sizeof(int), cudaMemcpyDeviceToHost);
     if (ce != cudaSuccess) return e->cuda_fail(ce, "synchronize");
-    if (flag) return e->fail(F3D_E_CUDA, "FFT3DCL: a tensor-core wait timed out; results since the last check are invalid");
+    if (flag) {
+      std::string which;
+      if (flag & kErrWaitForward) which += ", forward transform (tensor-core steps)";
+      if (flag & kErrWaitTile) which += ", inverse kernel (operand tile copy)";
+      if (flag & kErrWaitColumn) which += ", inverse kernel (column-inverse products)";
+      if (flag & kErrWaitRow) which += ", inverse kernel (row-inverse products)";
+      cudaMemset(e->d_err, 0, sizeof(int));
+      return e->fail(F3D_E_CUDA, "FFT3DCL: a tensor-core wait timed out: " + which.substr(2) +
+                                     "; the outputs since the last check are invalid");
+    }
   }
   return F3D_OK;
 }
@@ -968,6 +981,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
     if (!dev_dst[i] || dst_pitch[i] < (size_t)e->geom.width * e->bps)
       return batch_fail(b, F3D_E_PARAM, "FFT3DCL: bad output plane in batch");
     sa[ns] = sweep_args(e, a, static_cast<uint8_t*>(dev_dst[i]), (long long)dst_pitch[i], e->fmt);
+    e->test_skip = false;
     if (b->img[i]) {  // a repeated engine: this output's own tiles and seam rows
       sa[ns].img = b->img[i];
       sa[ns].seam_b = b->seam[i];
@@ -1188,6 +1202,7 @@ int engines_step(f3d_engine* const* eng, int n, const int* fns, const void* cons
     if (!dst[i] || dst_pitch[i] < (size_t)e->geom.width * e->bps)
       return bad(F3D_E_PARAM, "FFT3DCL: bad output plane in a shared step");
     sa[ns++] = sweep_args(e, a, static_cast<uint8_t*>(dst[i]), (long long)dst_pitch[i], e->fmt);
+    e->test_skip = false;
   }
   cudaSetDevice(eng[0]->device);
   cudaError_t ce = nf ? launch_forward_tc_batch(fa, nf, TcTune{}, st) : cudaSuccess;

@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kTcThreads, kFwdMaxCtasPerSm) k_forward_tc(con
     // wait that gave up anywhere ends the sweep of groups for the whole CTA.
     if (tid == 0) tc::bulk_wait_read();
     if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
-      if (tid == 0) atomicOr(a.err, 1);
+      if (tid == 0) atomicOr(a.err, kErrWaitForward);
       break;
     }
     tc::fence_after_sync();
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(kTcThreads, kFwdMaxCtasPerSm) k_forward_tc(con
 
     // Step 2 done: A2's space is free for the staging area.
     if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
-      if (tid == 0) atomicOr(a.err, 1);
+      if (tid == 0) atomicOr(a.err, kErrWaitForward);
       break;
     }
     phase ^= 1;
@@ -735,7 +735,9 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
     tc::fence_async_smem();
     if (M0 < M1) {
       tc::mbar_expect_tx(&bar[0], S::TILE);
-      tc::bulk_load(sm + S::A2, tile_of(M0), S::TILE, &bar[0]);
+      // A test of the bounded wait leaves this copy out: nothing is then in
+      // flight on the barrier, the wait below gives up and the CTA leaves.
+      if (!(sa.test_skip && cta == 0)) tc::bulk_load(sm + S::A2, tile_of(M0), S::TILE, &bar[0]);
     }
   }
   tc::fence_before_sync();
@@ -749,7 +751,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
   for (int m = M0; m < M1; m++) {
     // Step 2' on the tensor cores once the operand tile is in: D2 = A2 * C2^T.
     if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
-      if (tid == 0) atomicOr(sa.err, 1);
+      if (tid == 0) atomicOr(sa.err, kErrWaitTile);
       break;
     }
     if (tid == 0) {
@@ -769,7 +771,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
       tc::mma_commit(&bar[1]);
     }
     if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
-      if (tid == 0) atomicOr(sa.err, 1);
+      if (tid == 0) atomicOr(sa.err, kErrWaitColumn);
       break;
     }
     tc::fence_after_sync();
@@ -819,7 +821,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
       tc::mma_commit(&bar[2]);
     }
     if (!__syncthreads_and(tc::mbar_wait(&bar[2], phase, kWaitNs))) {
-      if (tid == 0) atomicOr(sa.err, 1);
+      if (tid == 0) atomicOr(sa.err, kErrWaitRow);
       break;
     }
     phase ^= 1;

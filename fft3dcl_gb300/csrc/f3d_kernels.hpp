@@ -99,8 +99,17 @@ struct SweepArgs {
   float* seam_b;         // [segs-1][bh/2][seam_w]: first two quadrants of each seam cell, summed
   float* seam_t;         // [segs-1][2][bh/2][seam_w]: third and fourth quadrants
   const uint8_t* tab;    // tensor-core form: device copy of tc_tables()
-  int* err;              // tensor-core form: set non-zero when a wait gives up
+  int* err;              // tensor-core form: bits set when a wait gives up (kErrWait*)
   uint8_t* img;          // tensor-core form: filtered column-inverse operands, one tile per (row, strip)
+  int test_skip;         // tests only: the plane's first CTA skips its first operand-tile copy
+};
+
+// Bits of the tensor-core kernels' error word: which wait gave up.
+enum : int {
+  kErrWaitForward = 1,  // forward: a group's tensor-core steps
+  kErrWaitTile = 2,     // inverse: the operand tile copy
+  kErrWaitColumn = 4,   // inverse: the column-inverse products
+  kErrWaitRow = 8       // inverse: the row-inverse products
 };
 
 // Whether the sweep handles this geometry and form; its CTA grid; the seam
@@ -155,7 +164,7 @@ struct TcFwdArgs {
   const uint8_t* tab;  // device copy of tc_tables()
   float2* spec;        // out: nb x bh x fbw half spectra (__half2 pairs when half)
   int half;            // store the spectra as fp16 pairs
-  int* err;            // set non-zero when a tensor-core wait gives up
+  int* err;            // kErrWaitForward set when a tensor-core wait gives up
 };
 bool tc_supported(int mode, int bw, int bh, int bm);
 // DFT matrices (fp16 hi/lo, in the kernels' shared-memory operand layout)

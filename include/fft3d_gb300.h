@@ -113,6 +113,12 @@ typedef struct {
  * fp32; results are within the 8-bit tolerance of the fp32 path, not
  * bit-equal to it. The reference port ignores precision, so this is opt-in. */
 #define F3D_FLAG_HALF_SPECTRA 8
+/* Tests of the error path only: the next output of a fused tensor-core
+ * engine leaves out one operand-tile copy of its inverse kernel, so that the
+ * bounded wait for it gives up after its one-second limit with nothing in
+ * flight; the output is then invalid and f3d_synchronize reports the wait.
+ * Applies once. */
+#define F3D_FLAG_TEST_WAIT_TIMEOUT (1 << 20)
 
 typedef struct {
   int nblocks, fbw, ncols, nrows;
@@ -198,7 +204,9 @@ int f3d_process_device(f3d_engine* e, const int* window, int n, void* dev_dst, s
  * [lo, hi]; a negative bound is disabled. */
 int f3d_prune(f3d_engine* e, int lo, int hi);
 
-/* Wait for all queued work of the engine. */
+/* Wait for all queued work of the engine. F3D_E_CUDA when a tensor-core
+ * kernel's bounded wait gave up since the last call (the message names the
+ * wait; the outputs queued since are invalid); the report clears it. */
 int f3d_synchronize(f3d_engine* e);
 /* Device time of the kernels of the last forward / process calls in ms
  * (CUDA events on the engine stream; valid after f3d_synchronize):
