@@ -144,22 +144,28 @@ def make_clip(nframes: int = NFRAMES):
 
 # --------------------------------------------------------------- CPU leg --
 
-def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_steps: int = 1):
+def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_steps: int = 1,
+                     bits: int = BITS, params: dict | None = None):
     """Oracle (the C restatement of the reference CPU backend) in steady
     state: per step one new frame is uploaded and transformed, then the
-    window is filtered, inverted, overlap-added and downloaded. Returns
-    (frames/s, steps)."""
+    window is filtered, inverted, overlap-added and downloaded (Kalman:
+    the state carries over from step to step). Returns (frames/s, steps)."""
     import ctypes as C
     import oracle
+    params = PARAMS if params is None else params
     L = oracle.lib()
-    pl = oracle.Plane(W, H, BITS, **PARAMS)
+    h, w = frames[0].shape
+    st = 1 if frames[0].dtype == np.float32 else 0
+    pl = oracle.Plane(w, h, bits, st, **params)
     pl.build_degrid()
     n = pl.nb * pl.fbw * pl.ip.bh
-    bt, cur = pl.ip.bt, pl.ip.current
+    bm = pl.ip.bm
+    bt = pl.ip.bt if bm >= 2 else 1
+    cur = pl.ip.current if bm >= 2 else 0
     slots = [(np.empty(n, np.float32), np.empty(n, np.float32)) for _ in range(bt + 1)]
-    plane = np.empty((H, W), np.float32)
-    out = np.empty((H, W), np.float32)
-    dst = np.empty((H, W), np.uint16)
+    plane = np.empty((h, w), np.float32)
+    out = np.empty((h, w), np.float32)
+    dst = np.empty((h, w), frames[0].dtype)
 
     def spectra(fn, slot):
         f = frames[fn % len(frames)]
@@ -171,8 +177,8 @@ def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_
         new = nout - cur + bt - 1
         spectra(new, slots[new % (bt + 1)])
         win = [slots[(nout - cur + i) % (bt + 1)] for i in range(bt)]
-        wr = (C.c_void_p * bt)(*[w[0].ctypes.data for w in win])
-        wi = (C.c_void_p * bt)(*[w[1].ctypes.data for w in win])
+        wr = (C.c_void_p * bt)(*[x[0].ctypes.data for x in win])
+        wi = (C.c_void_p * bt)(*[x[1].ctypes.data for x in win])
         L.orc_filter_and_synthesize(pl.h, wr, wi, bt, oracle._ptr(out), threads)
         L.orc_download(pl.h, oracle._ptr(out), oracle._ptr(dst), dst.strides[0])
 
@@ -186,6 +192,93 @@ def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_
         steps += 1
     dt = time.perf_counter() - t0
     return steps / dt, steps
+
+
+# The two other single-plane workloads: the plain method on 640x360 GRAY8
+# and Kalman on 1280x720 float with the sigma pattern and scene cuts.
+GRAY8_PARAMS = dict(sigma=2.0, beta=1.0, bt=3, bw=32, bh=32, ow=16, oh=16, degrid=1.0, sharpen=0.0)
+KALMAN_PARAMS = dict(bt=0, kratio=2.0, bw=64, bh=64, ow=32, oh=32, sigma=2.0, sigma2=1.5, sigma3=2.5, sigma4=3.0)
+# Algorithmic bytes per output frame with resident spectra: 640x360 GRAY8
+# bt=3: 2 x 230,400 + 4,386,816 x (1 + 3); 720p float Kalman: 2 x 3,686,400
+# + 2 x 16 B of state x 2,128,896 bins.
+AB_GRAY8 = 2 * 640 * 360 + 1008 * 17 * 32 * 8 * 4
+AB_KALMAN = 2 * 1280 * 720 * 4 + 2 * 16 * 1008 * 33 * 64
+
+
+def config_section(args, dev, local_rank, frames, bits, params, forms, ab_bytes, peak, kbatch=1):
+    """Device throughput of one single-plane workload in steady state with the
+    clip resident in HBM (engine calls per output; for the tensor-core form
+    also batch steps of kbatch consecutive outputs, CUDA graph), its step
+    roofline on algorithmic bytes, and the oracle on the host's threads over
+    a bounded sample."""
+    import torch
+    import fft3dcl_gb300 as F
+    h, w = frames[0].shape
+    st = 1 if frames[0].dtype == np.float32 else 0
+    bps = frames[0].itemsize
+    clip = torch.from_numpy(np.stack(frames)).to(dev)
+    nfr = clip.shape[0]
+    ip = F.validate(w, h, bits, **params)
+    bm = ip.bm
+    need = ip.bt if bm >= 2 else 1
+    cur = ip.current if bm >= 2 else 0
+    pitch = w * bps
+    res = {}
+    for form, k in [(f, 1) for f in forms] + ([("tc", kbatch)] if kbatch > 1 and "tc" in forms else []):
+        stream = torch.cuda.Stream(device=dev)
+        eng = F.Engine(w, h, bits, st, form=form, device=local_rank, stream=stream.cuda_stream, **params)
+        outs = [torch.empty((h, w), dtype=clip.dtype, device=dev) for _ in range(k)]
+        batch = F.Batch([eng] * k, graph=True, autotune=True) if k > 1 else None
+
+        def step(n):
+            wins = [[m - cur + i for i in range(need)] for m in range(n, n + k)]
+            for wnd in wins:  # only the first step finds frames missing
+                for fn in wnd:
+                    if not eng.has(fn):
+                        eng.forward_device(fn, clip[fn % nfr].data_ptr(), pitch)
+            if batch is None:
+                eng.process_device(wins[0], outs[0].data_ptr(), pitch)
+            else:
+                # The frames the next step's windows add, forwarded in this
+                # step concurrently with its outputs.
+                ahead = [n + k - 1 - cur + need + i for i in range(k)]
+                batch.step(ahead, [clip[a % nfr].data_ptr() for a in ahead], [pitch] * k, wins,
+                           [o.data_ptr() for o in outs], [pitch] * k)
+            if bm == 0:  # Kalman keeps only the current frame
+                eng.prune(n + k - 1, n + k - 1)
+            else:
+                eng.prune(n - cur - 1, n + 2 * k - 1 - cur + need)
+
+        n = max(cur, 1)
+        for _ in range(max(3, args.warmup)):
+            step(n)
+            n += k
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(n)
+            n += k
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        fps = args.steps * k / (e0.elapsed_time(e1) / 1000.0)
+        info = eng.info()
+        key = form if k == 1 else f"{form}_batch{k}"
+        res[key] = {"frames_per_s": round(fps, 1), "form_run": ["exact", "fast", "tc"][info.form],
+                    "roofline_step": {"algorithmic_bytes": ab_bytes, "achieved": round(ab_bytes * fps / 1e9, 1),
+                                      "unit": "GB/s", "frac": round(ab_bytes * fps / 1e9 / peak, 4)}}
+        if batch is not None:
+            res[key]["how"] = (f"batch steps of {k} consecutive outputs, the next step's frames forwarded "
+                               "concurrently, CUDA graph replay, autotuned launch shape")
+            batch.close()
+        eng.close()
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        fps_cpu, steps = cpu_steady_state(frames, threads, 5.0, 200, bits=bits, params=params)
+        res["cpu_baseline"] = {"value": round(fps_cpu, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"{steps} steady-state output frames (about 5 s) on {threads} host "
+                                         "threads, C restatement of src/cpu, bit-identical to the reference"}
+    return res
 
 
 YUV_PARAMS = dict(sigma=2.5, bt=4, bw=32, bh=32, ow=16, oh=16, sharpen=0.4, scutoff=0.3, svr=1.0, smin=4.0,
@@ -609,6 +702,19 @@ def run_gpu(args, rank, world, local_rank):
         line["yuv1080p_all_planes"] = dict(
             workload="1920x1080 YUV420P8 all planes, sigma=2.5 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4 scutoff=0.3 "
                      "svr=1 smin=4 smax=20 degrid=1, clip resident in HBM", **yuv_batched(args, dev, local_rank))
+    if world == 1 and not args.no_configs:
+        from fft3dcl_gb300 import synth
+        line["gray8_640x360_bt3"] = dict(
+            workload="640x360 GRAY8, 16-frame clip, sigma=2 beta=1 bt=3 bw=bh=32 ow=oh=16 degrid=1 sharpen=0 "
+                     "(the plain method), clip resident in HBM",
+            **config_section(args, dev, local_rank, synth.clip_gray8(), 8, GRAY8_PARAMS, ("exact", "fast", "tc"),
+                             AB_GRAY8, peak, kbatch=16))
+        line["grays_1280x720_kalman_bw64"] = dict(
+            workload="1280x720 GRAYS float, 64-frame clip with scene cuts at 20 and 45, Kalman bt=0 kratio=2 "
+                     "bw=bh=64 ow=oh=32, sigma pattern 2/1.5/2.5/3, state resident in HBM (Kalman runs the exact "
+                     "form in every form)",
+            **config_section(args, dev, local_rank, synth.clip_grays(), 32, KALMAN_PARAMS, ("exact",), AB_KALMAN,
+                             peak))
     if world == 1 and args.serve_streams > 0:
         # The serving workload: YUV 4:2:0 video streams (all planes) with
         # Poisson frame arrivals through the serving loop (shared steps for
@@ -682,6 +788,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-streams", type=int, default=16, help="streams of the serving run (0: skip it)")
     ap.add_argument("--no-yuv", action="store_true", help="skip the batched 1080p YUV measurement")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 640x360 GRAY8 and 720p float Kalman measurements")
     ap.add_argument("--no-batch", action="store_true",
                     help="tensor-core headline through the engine's own calls instead of a batch step")
     ap.add_argument("--outputs-per-step", type=int, default=DEFAULT_OUTPUTS_PER_STEP, choices=list(range(1, 17)),

@@ -29,3 +29,14 @@ def test_default_batch_step_has_measured_filter_traffic():
     # k outputs' operand tiles: below the k x 4 spectra of algorithmic reads.
     spec = 143233024
     assert (k + 3) * spec * 0.95 < traffic < k * 4 * spec
+
+
+def test_algorithmic_bytes_of_the_other_workloads():
+    # Block counts and spectrum sizes from the oracle's own geometry.
+    import oracle
+    g = oracle.Plane(640, 360, 8, **bench.GRAY8_PARAMS)
+    spec = g.nb * g.fbw * g.ip.bh * 8
+    assert bench.AB_GRAY8 == 2 * 640 * 360 + spec * (1 + 3) == 18008064
+    k = oracle.Plane(1280, 720, 32, 1, **bench.KALMAN_PARAMS)
+    bins = k.nb * k.fbw * k.ip.bh
+    assert bench.AB_KALMAN == 2 * 1280 * 720 * 4 + 2 * 16 * bins == 75497472
