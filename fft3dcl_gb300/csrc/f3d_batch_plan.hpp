@@ -41,28 +41,29 @@ inline bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepB
       return false;
     B.p[i] = a;
   }
+  // Runs of consecutive planes of one geometry (the same group and segment
+  // counts). A run of consecutive outputs of one plane is shifted: every
+  // window frame but the newest is the previous entry's (the same spectrum
+  // buffers). The filter kernel interleaves the CTAs of a run's planes.
+  const int nf = B.p[0].inv.bm >= 2 ? B.p[0].inv.bm : 1;
+  B.shifted = 0;
+  for (int i = 0; i < n; i++) {
+    const SweepArgs& a = B.p[i];
+    const bool same = i > 0 && a.inv.g.W == B.p[i - 1].inv.g.W && a.inv.g.H == B.p[i - 1].inv.g.H &&
+                      a.strips == B.p[i - 1].strips && a.segs == B.p[i - 1].segs;
+    B.run[i] = same ? B.run[i - 1] : i;
+    B.rlen[i] = 0;
+    B.rlen[B.run[i]]++;
+    bool shift = same && nf > 1;
+    for (int k = 0; k + 1 < nf && shift; k++) shift = a.inv.s[k] == B.p[i - 1].inv.s[k + 1];
+    if (shift) B.shifted |= 1 << i;
+  }
   auto prefix = [&](SweepBatch& out, auto count) {
     out = B;
     for (int i = 0; i < n; i++) out.cta0[i + 1] = out.cta0[i] + count(out.p[i]);
     for (int i = n + 1; i <= kMaxBatch; i++) out.cta0[i] = out.cta0[n];
   };
   prefix(Bf, [](const SweepArgs& a) { return a.strips * (a.cells_y + 1); });  // (row, strip) groups
-  // Runs of consecutive planes of one geometry (the same group count). A run
-  // of consecutive outputs of one plane is shifted: every window frame but
-  // the newest is the previous entry's (the same spectrum buffers).
-  const int nf = B.p[0].inv.bm >= 2 ? B.p[0].inv.bm : 1;
-  Bf.shifted = 0;
-  for (int i = 0; i < n; i++) {
-    const SweepArgs& a = B.p[i];
-    const bool same = i > 0 && a.inv.g.W == B.p[i - 1].inv.g.W && a.inv.g.H == B.p[i - 1].inv.g.H &&
-                      a.strips == B.p[i - 1].strips;
-    Bf.run[i] = same ? Bf.run[i - 1] : i;
-    Bf.rlen[i] = 0;
-    Bf.rlen[Bf.run[i]]++;
-    bool shift = same && nf > 1;
-    for (int k = 0; k + 1 < nf && shift; k++) shift = a.inv.s[k] == B.p[i - 1].inv.s[k + 1];
-    if (shift) Bf.shifted |= 1 << i;
-  }
   prefix(Bs, [](const SweepArgs& a) { return a.strips * a.segs; });          // (strip, segment)
   prefix(Bm, [](const SweepArgs& a) { return a.segs > 1 ? a.segs - 1 : 0; });  // seams
   return true;

@@ -540,20 +540,19 @@ __device__ __forceinline__ float2 spec_at(const float2* s, size_t j) {
   else return s[j];
 }
 
-// R. Row (k', block), K = 2 ky + (re, im) of the operand image of group
-// (m, strip) from its filtered bins fbuf[block][bin], in 16-byte chunks of 4
-// ky. Block 0 also goes to the previous strip's tile as its block 7; this
-// tile's block 7 comes from the next strip.
+// R. Row (k', block), K = 2 ky + (re, im) of the operand image of a group
+// from its filtered bins fbuf[block][bin], in 16-byte chunks of 4 ky, into
+// img. prev (optional) also receives block 0, as the previous strip's block
+// 7; with skip_last the group's block 7 is not written (the next strip
+// writes it).
 template <int N>
-__device__ __forceinline__ void operand_tile(const SweepArgs& sa, int m, int strip, const float2* fbuf, int tid) {
+__device__ __forceinline__ void tile_rows(uint8_t* img, uint8_t* prev, bool skip_last, const float2* fbuf,
+                                          int tid) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
-  const bool last_strip = strip == sa.strips - 1;
-  uint8_t* img = sa.img + ((size_t)m * sa.strips + strip) * S::TILE;
-  uint8_t* prev = strip > 0 ? img - S::TILE : nullptr;
   const int r2 = tid & 127, h = tid >> 7;
   const int kp = r2 >> 3, bl = r2 & 7;
-  if (bl == C::G - 1 && !last_strip) return;
+  if (bl == C::G - 1 && skip_last) return;
   const float2* fb = fbuf + bl * S::FS;
 #pragma unroll
   for (int cq = 0; cq < C::NY / 4; cq++) {
@@ -585,74 +584,65 @@ __device__ __forceinline__ void operand_tile(const SweepArgs& sa, int m, int str
   }
 }
 
-template <int N, int BM, int MINB, bool HALF>
-__global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_constant__ SweepBatch B) {
-  using C = TcCfg<N>;
+// The operand image of group (m, strip) in HBM: block 0 also goes to the
+// previous strip's tile as its block 7; this tile's block 7 comes from the
+// next strip.
+template <int N>
+__device__ __forceinline__ void operand_tile(const SweepArgs& sa, int m, int strip, const float2* fbuf, int tid) {
   using S = SwpCfg<N>;
-  constexpr int kTcFilterBatch = filter_batch(MINB);
-  // A run of planes of one geometry (e.g. consecutive frames of a plane)
-  // runs the same group of each of its planes back to back, so that the
-  // window spectra they share are read from L2 the second time.
-  const int r0 = B.run[plane_of(B, B.cta0, blockIdx.x)];
-  const int rl = B.rlen[r0];
-  const int local = (int)blockIdx.x - B.cta0[r0];
-  const int pl = r0 + local % rl;
-  const SweepArgs& sa = B.p[pl];
-  const int cta = local / rl;
-  const InvArgs& a = sa.inv;
-  extern __shared__ __align__(16) uint8_t smem_f[];
-  float2* fbuf = reinterpret_cast<float2*>(smem_f);
-  float* dcs = reinterpret_cast<float*>(smem_f + S::F_DC);
-  const int tid = threadIdx.x;
-  const int strip = cta % sa.strips, m = cta / sa.strips;
-  const int J0 = strip * S::TJ;
-  const int ncols = a.g.ncols;
-  // A tile's eighth block is the next strip's first: that strip filters it
-  // and writes it into both tiles, so each block is filtered once. The last
-  // strip filters its own eighth block.
-  const bool last_strip = strip == sa.strips - 1;
-  const int own = last_strip ? C::G : C::G - 1;
-  const int nvbin = max(0, min(own, min(sa.cells_x + 1, ncols) - J0)) * C::PS;  // bins filtered here
-  constexpr int NF = BM >= 2 ? BM : 1;  // window frames read
+  uint8_t* img = sa.img + ((size_t)m * sa.strips + strip) * S::TILE;
+  tile_rows<N>(img, strip > 0 ? img - S::TILE : nullptr, strip != sa.strips - 1, fbuf, tid);
+}
 
-  const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
-  // The group's window spectra start moving into L2 as whole runs, so that
-  // the bins' loads below mostly wait on L2 rather than on DRAM. Of shifted
-  // windows (consecutive outputs, their CTAs side by side), each later output
-  // pulls only its newest frame: the others are an earlier output's.
+// Start of a group's filter: its window spectra begin moving into L2 as
+// whole runs (of shifted windows, only the newest frame: the others are an
+// earlier output's), and the current frame's DC of each block (the degrid
+// correction's scale) goes to dcs. gb0: the group's first bin; nvbin: the
+// bins filtered.
+template <int N, int NF, bool HALF>
+__device__ __forceinline__ void group_start(const SweepArgs& sa, size_t gb0, int nvbin, bool shifted, int m, int J0,
+                                            float* dcs, int tid) {
+  using C = TcCfg<N>;
+  const InvArgs& a = sa.inv;
   constexpr uint32_t BIN_BYTES = HALF ? 4 : 8;
-  const bool pull = !((B.shifted >> pl) & 1) || tid == NF - 1;
+  const bool pull = !shifted || tid == NF - 1;
   if (tid < NF && nvbin > 0 && pull)
     tc::prefetch_l2(reinterpret_cast<const uint8_t*>(a.s[tid]) + gb0 * BIN_BYTES, (uint32_t)(nvbin * BIN_BYTES));
   if (tid < C::G) {
     const int n = J0 + tid;
-    dcs[tid] = (a.dg && n <= sa.cells_x && n < ncols)
-                   ? spec_at<HALF>(a.s[a.cur], (size_t)(m * ncols + n) * C::PS).x
+    dcs[tid] = (a.dg && n <= sa.cells_x && n < a.g.ncols)
+                   ? spec_at<HALF>(a.s[a.cur], (size_t)(m * a.g.ncols + n) * C::PS).x
                    : 0.0f;
   }
-  __syncthreads();
+}
 
-  // F. Thread t filters bin li = t + 256 r (r < NL) of every block of the
-  // group, the bin's tables read once for all blocks, then tail item q: bin
-  // NL * 256 + e % TAIL of block e / TAIL, e = t + 256 q. The spectra loads of
-  // kTcFilterBatch blocks are issued together; every index is the thread's
-  // base plus a constant.
+// F. The temporal filter (filter_vals, fast form) of a group's nvb blocks
+// into fbuf[block][bin] (blocks nvb.. get zeros). Thread t filters bin
+// li = t + 256 r (r < NL) of every block of the group, the bin's tables read
+// once for all blocks, then tail item q: bin NL * 256 + e % TAIL of block
+// e / TAIL, e = t + 256 q. The spectra loads of BATCH blocks are issued
+// together; every index is the thread's base plus a constant.
+template <int N, int BM, int BATCH, bool HALF>
+__device__ __forceinline__ void filter_group(const InvArgs& a, size_t gb0, int nvb, const float* dcs, float2* fbuf,
+                                             int tid) {
+  using C = TcCfg<N>;
+  using S = SwpCfg<N>;
+  constexpr int NF = BM >= 2 ? BM : 1;
   constexpr int NL = C::PS / kTcThreads;
   constexpr int TAIL = C::PS - NL * kTcThreads;
   constexpr int NT = TAIL * C::G / kTcThreads;
   static_assert((TAIL * C::G) % kTcThreads == 0, "tail bins per thread");
-  static_assert(C::G % kTcFilterBatch == 0, "load batches");
-  const int nvb = nvbin / C::PS;  // blocks filtered here
+  static_assert(C::G % BATCH == 0, "load batches");
   const size_t gt = gb0 + tid;
   if constexpr (NL > 0) {
     BinTables tb[NL];
 #pragma unroll
     for (int r = 0; r < NL; r++) tb[r] = bin_tables(a, tid + kTcThreads * r);
 #pragma unroll
-    for (int b0 = 0; b0 < C::G; b0 += kTcFilterBatch) {
-      float2 sv[kTcFilterBatch][NL][4];
+    for (int b0 = 0; b0 < C::G; b0 += BATCH) {
+      float2 sv[BATCH][NL][4];
 #pragma unroll
-      for (int u = 0; u < kTcFilterBatch; u++) {
+      for (int u = 0; u < BATCH; u++) {
         if (b0 + u >= nvb) continue;
 #pragma unroll
         for (int r = 0; r < NL; r++)
@@ -661,7 +651,7 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
             sv[u][r][k] = spec_at<HALF>(a.s[k], gt + (size_t)(b0 + u) * C::PS + kTcThreads * r);
       }
 #pragma unroll
-      for (int u = 0; u < kTcFilterBatch; u++) {
+      for (int u = 0; u < BATCH; u++) {
         const int b = b0 + u;
         const float dc = dcs[b];
 #pragma unroll
@@ -687,22 +677,259 @@ __global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_con
     }
     fbuf[b * S::FS + li] = f;
   }
+}
+
+template <int N, int BM, int MINB, bool HALF>
+__global__ void __launch_bounds__(kTcThreads, MINB) k_filter_tc(const __grid_constant__ SweepBatch B) {
+  using C = TcCfg<N>;
+  using S = SwpCfg<N>;
+  // A run of planes of one geometry (e.g. consecutive frames of a plane)
+  // runs the same group of each of its planes back to back, so that the
+  // window spectra they share are read from L2 the second time.
+  const int r0 = B.run[plane_of(B, B.cta0, blockIdx.x)];
+  const int rl = B.rlen[r0];
+  const int local = (int)blockIdx.x - B.cta0[r0];
+  const int pl = r0 + local % rl;
+  const SweepArgs& sa = B.p[pl];
+  const int cta = local / rl;
+  const InvArgs& a = sa.inv;
+  extern __shared__ __align__(16) uint8_t smem_f[];
+  float2* fbuf = reinterpret_cast<float2*>(smem_f);
+  float* dcs = reinterpret_cast<float*>(smem_f + S::F_DC);
+  const int tid = threadIdx.x;
+  const int strip = cta % sa.strips, m = cta / sa.strips;
+  const int J0 = strip * S::TJ;
+  const int ncols = a.g.ncols;
+  // A tile's eighth block is the next strip's first: that strip filters it
+  // and writes it into both tiles, so each block is filtered once. The last
+  // strip filters its own eighth block.
+  const bool last_strip = strip == sa.strips - 1;
+  const int own = last_strip ? C::G : C::G - 1;
+  const int nvb = max(0, min(own, min(sa.cells_x + 1, ncols) - J0));  // blocks filtered here
+  constexpr int NF = BM >= 2 ? BM : 1;  // window frames read
+  const size_t gb0 = ((size_t)m * ncols + J0) * C::PS;
+  group_start<N, NF, HALF>(sa, gb0, nvb * C::PS, (B.shifted >> pl) & 1, m, J0, dcs, tid);
+  __syncthreads();
+  filter_group<N, BM, filter_batch(MINB), HALF>(a, gb0, nvb, dcs, fbuf, tid);
+  __syncthreads();
+  operand_tile<N>(sa, m, strip, fbuf, tid);
+}
+
+// Shared-memory and barrier state of the inverse phases of one CTA.
+struct InvState {
+  uint8_t* sm;
+  uint32_t sbase;
+  uint64_t* bar;  // [1] column-inverse products, [2] row-inverse products
+  uint32_t tmem;
+  uint32_t phase;
+  float* P_old;   // cell partial sums of block row m - 1 (finished by this row's top halves)
+  float* P_new;   // cell partial sums of block row m
+};
+
+// The inverse of block row m once its operand tile is in shared memory (A2):
+// step 2' (column inverse, tensor cores), V, step 1' (row inverse with the
+// synthesis windows, tensor cores), then `after` (the tile's space is free
+// again), then O (overlap-add in the reference's block order, finished cell
+// rows packed to the output, segment seams). Returns false when a wait gave
+// up (the error word has its bit); every thread of the CTA returns the same.
+template <int N, class After>
+__device__ __forceinline__ bool inverse_row(const SweepArgs& sa, InvState& st, int m, int M0, int M1, int seg, int J0,
+                                            int ncell, After after) {
+  using C = TcCfg<N>;
+  using S = SwpCfg<N>;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint8_t* sm = st.sm;
+  const uint32_t sbase = st.sbase;
+  uint64_t* bar = st.bar;
+  const uint32_t tmem = st.tmem;
+  if (tid == 0) {
+    tc::fence_after_sync();
+    constexpr uint32_t id2 = tc::idesc_f16(128, C::N2);
+    const uint32_t sbo_b = (C::K2 / 8) * 128;
+    const uint32_t d = tmem + C::D2_COL;
+    for (int ks = 0; ks < C::K2 / 16; ks++) {
+      const uint64_t ah = tc::sdesc(sbase + S::A2 + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+      const uint64_t al = tc::sdesc(sbase + S::A2 + C::A2_BYTES + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+      const uint64_t bh = tc::sdesc(sbase + S::C2 + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
+      const uint64_t bl = tc::sdesc(sbase + S::C2 + C::B2_BYTES + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
+      tc::mma_f16(d, ah, bh, id2, ks > 0);
+      tc::mma_f16(d, ah, bl, id2, 1);
+      tc::mma_f16(d, al, bh, id2, 1);
+    }
+    tc::mma_commit(&bar[1]);
+  }
+  if (!__syncthreads_and(tc::mbar_wait(&bar[1], st.phase, kWaitNs))) {
+    if (tid == 0) atomicOr(sa.err, kErrWaitColumn);
+    return false;
+  }
+  tc::fence_after_sync();
+
+  // V. Row-inverse operand: tile = parity of the block column, row (y, slot).
+  {
+    const int s = warp & 3, h = warp >> 2;
+    const int r2 = 32 * s + lane;
+    const int kp = r2 >> 3, bl = r2 & 7;
+    const int tile = (J0 + bl) & 1, slot = bl >> 1;
+    uint8_t* t0 = sm + S::A1 + tile * S::A1_STRIDE;
+    float v[32];
+    tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + 32 * h, v);
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int y = 16 * h + j;
+      uint32_t hi, lo;
+      tc::split_pair(v[2 * j], v[2 * j + 1], hi, lo);
+      const uint32_t o = tc::off_il(4 * y + slot, 2 * kp, C::K1);
+      *reinterpret_cast<uint32_t*>(t0 + o) = hi;
+      *reinterpret_cast<uint32_t*>(t0 + C::A1_BYTES + o) = lo;
+    }
+  }
+  tc::fence_async_smem();
+  tc::fence_before_sync();
   __syncthreads();
 
-  operand_tile<N>(sa, m, strip, fbuf, tid);
+  // Step 1' on the tensor cores: D1[tile] = A1[tile] * C1(tile)^T.
+  if (tid == 0) {
+    tc::fence_after_sync();
+    constexpr uint32_t id1 = tc::idesc_f16(128, C::N1);
+    const uint32_t sbo = (C::K1 / 8) * 128;
+    for (int t = 0; t < C::T1; t++) {
+      const uint32_t a_hi = sbase + S::A1 + t * S::A1_STRIDE, a_lo = a_hi + C::A1_BYTES;
+      const uint32_t b_hi = sbase + S::C1 + t * 2 * C::B1_BYTES, b_lo = b_hi + C::B1_BYTES;
+      const uint32_t d = tmem + C::D1_COL + t * C::N1;
+      for (int ks = 0; ks < C::K1 / 16; ks++) {
+        const uint64_t ah = tc::sdesc(a_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+        const uint64_t al = tc::sdesc(a_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+        const uint64_t bh = tc::sdesc(b_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+        const uint64_t bl = tc::sdesc(b_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
+        tc::mma_f16(d, ah, bh, id1, ks > 0);
+        tc::mma_f16(d, ah, bl, id1, 1);
+        tc::mma_f16(d, al, bh, id1, 1);
+      }
+    }
+    tc::mma_commit(&bar[2]);
+  }
+  if (!__syncthreads_and(tc::mbar_wait(&bar[2], st.phase, kWaitNs))) {
+    if (tid == 0) atomicOr(sa.err, kErrWaitRow);
+    return false;
+  }
+  st.phase ^= 1;
+  tc::fence_after_sync();
+  after();
+
+  // O. Overlap-add. Thread: block row y of block bl; y < n/2 finishes cell
+  // row m-1 (P_old), y >= n/2 starts cell row m (P_new).
+  float* P_old = st.P_old;
+  float* P_new = st.P_new;
+  {
+    const int t = warp >> 2, s = warp & 3;
+    const int r = 32 * s + lane;
+    const int y = r >> 2, slot = r & 3;
+    const int bl = 2 * slot + ((t ^ J0) & 1);
+    float v[32];
+    tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
+#pragma unroll
+    for (int x = 0; x < 32; x++) v[x] *= out_scale<N>();
+    const bool top = y < S::CH;
+    const int yy = top ? y : y - S::CH;
+    const bool right_ok = bl < ncell;                // right half -> cell bl
+    const bool left_ok = bl >= 1 && bl - 1 < ncell;  // left half -> cell bl-1
+    const bool seam_top = m == M0;                   // cell row m-1 is another segment's (or none)
+    if (top) {
+      if (seam_top) {
+        if (M0 > 0 && right_ok) {
+          float* t0 = sa.seam_t + ((size_t)((seg - 1) * 2) * S::CH + yy) * sa.seam_w + (J0 + bl) * S::CW;
+#pragma unroll
+          for (int x = 0; x < S::CW; x += 4)
+            *reinterpret_cast<float4*>(t0 + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
+        }
+      } else if (right_ok) {
+        float* p = P_old + bl * S::PC + yy * S::PR;
+#pragma unroll
+        for (int x = 0; x < S::CW; x += 4) {
+          float4 q = *reinterpret_cast<float4*>(p + x);
+          q.x += v[16 + x], q.y += v[17 + x], q.z += v[18 + x], q.w += v[19 + x];
+          *reinterpret_cast<float4*>(p + x) = q;
+        }
+      }
+    } else if (right_ok) {
+      float* p = P_new + bl * S::PC + yy * S::PR;
+#pragma unroll
+      for (int x = 0; x < S::CW; x += 4)
+        *reinterpret_cast<float4*>(p + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
+    }
+    __syncthreads();
+    if (top) {
+      if (seam_top) {
+        if (M0 > 0 && left_ok) {
+          float* t1 = sa.seam_t + ((size_t)((seg - 1) * 2 + 1) * S::CH + yy) * sa.seam_w + (J0 + bl - 1) * S::CW;
+#pragma unroll
+          for (int x = 0; x < S::CW; x += 4)
+            *reinterpret_cast<float4*>(t1 + x) = make_float4(v[x], v[x + 1], v[x + 2], v[x + 3]);
+        }
+      } else if (left_ok) {
+        const float* p = P_old + (bl - 1) * S::PC + yy * S::PR;
+        float o[16];
+#pragma unroll
+        for (int x = 0; x < S::CW; x += 4) {
+          const float4 q = *reinterpret_cast<const float4*>(p + x);
+          o[x] = q.x + v[x], o[x + 1] = q.y + v[x + 1], o[x + 2] = q.z + v[x + 2], o[x + 3] = q.w + v[x + 3];
+        }
+        emit16(sa, (m - 1) * S::CH + yy, (J0 + bl - 1) * S::CW, o);
+      }
+    } else if (left_ok) {
+      float* p = P_new + (bl - 1) * S::PC + yy * S::PR;
+      const bool seam_bot = m == M1 - 1 && seg < sa.segs - 1;
+      float* sb = sa.seam_b + ((size_t)seg * S::CH + yy) * sa.seam_w + (J0 + bl - 1) * S::CW;
+#pragma unroll
+      for (int x = 0; x < S::CW; x += 4) {
+        float4 q = *reinterpret_cast<float4*>(p + x);
+        q.x += v[x], q.y += v[x + 1], q.z += v[x + 2], q.w += v[x + 3];
+        if (seam_bot) *reinterpret_cast<float4*>(sb + x) = q;
+        else *reinterpret_cast<float4*>(p + x) = q;
+      }
+    }
+  }
+  st.P_old = P_new;
+  st.P_new = P_old;
+  tc::fence_before_sync();
+  __syncthreads();
+  return true;
+}
+
+// Constant operands of the inverse (C2 hi, lo, then C1 A hi, lo, B hi, lo)
+// into shared memory, tensor memory and the barriers.
+template <int N>
+__device__ __forceinline__ void inverse_setup(const SweepArgs& sa, uint8_t* sm, uint64_t* bar, uint32_t* tslot) {
+  using C = TcCfg<N>;
+  using S = SwpCfg<N>;
+  using T = TcTab<N>;
+  const int tid = threadIdx.x;
+  const uint4* src2 = reinterpret_cast<const uint4*>(sa.tab + T::C2HI);
+  uint4* dst2 = reinterpret_cast<uint4*>(sm + S::C2);
+  for (int i = tid; i < (int)(2 * C::B2_BYTES / 16); i += kTcThreads) dst2[i] = src2[i];
+  const uint4* src1 = reinterpret_cast<const uint4*>(sa.tab + T::C1AHI);
+  uint4* dst1 = reinterpret_cast<uint4*>(sm + S::C1);
+  for (int i = tid; i < (int)(4 * C::B1_BYTES / 16); i += kTcThreads) dst1[i] = src1[i];
+  if ((tid >> 5) == 0) {
+    tc::tmem_alloc(tslot, C::TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 3; i++) tc::mbar_init(&bar[i], 1);
+    tc::fence_mbar_init();
+  }
 }
 
 template <int N>
 __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(const __grid_constant__ SweepBatch B) {
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
-  using T = TcTab<N>;
+  static_assert(sizeof(B) <= 32000, "kernel parameter space");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
-  const uint32_t sbase = tc::smem_u32(sm);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + S::BAR);  // [0] operand load, [1] step 2', [2] step 1'
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S::TSLOT);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5;
 
   const int pl = plane_of(B, B.cta0, blockIdx.x);
   const SweepArgs& sa = B.p[pl];
@@ -715,23 +942,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
   const int ncell = min(S::TJ, sa.cells_x - J0);
   auto tile_of = [&](int m) { return sa.img + ((size_t)m * sa.strips + strip) * S::TILE; };
 
-  // Constant operands: C2 (hi, lo), then C1 A (hi, lo) and B (hi, lo).
-  {
-    const uint4* src2 = reinterpret_cast<const uint4*>(sa.tab + T::C2HI);
-    static_assert(sizeof(B) <= 32000, "kernel parameter space");
-    uint4* dst2 = reinterpret_cast<uint4*>(sm + S::C2);
-    for (int i = tid; i < (int)(2 * C::B2_BYTES / 16); i += kTcThreads) dst2[i] = src2[i];
-    const uint4* src1 = reinterpret_cast<const uint4*>(sa.tab + T::C1AHI);
-    uint4* dst1 = reinterpret_cast<uint4*>(sm + S::C1);
-    for (int i = tid; i < (int)(4 * C::B1_BYTES / 16); i += kTcThreads) dst1[i] = src1[i];
-  }
-  if (warp == 0) {
-    tc::tmem_alloc(tslot, C::TMEM_COLS);
-    tc::tmem_relinquish();
-  }
+  inverse_setup<N>(sa, sm, bar, tslot);
   if (tid == 0) {
-    for (int i = 0; i < 3; i++) tc::mbar_init(&bar[i], 1);
-    tc::fence_mbar_init();
     tc::fence_async_smem();
     if (M0 < M1) {
       tc::mbar_expect_tx(&bar[0], S::TILE);
@@ -743,177 +955,30 @@ __global__ void __launch_bounds__(kTcThreads, kTcSweepCtasPerSm) k_sweep_tc(cons
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  const uint32_t tmem = *tslot;
-  uint32_t phase = 0;
-  float* P_old = reinterpret_cast<float*>(sm + S::P);
-  float* P_new = P_old + S::TJ * S::PC;
+  InvState st{sm, tc::smem_u32(sm), bar, *tslot, 0u, reinterpret_cast<float*>(sm + S::P),
+              reinterpret_cast<float*>(sm + S::P) + S::TJ * S::PC};
 
   for (int m = M0; m < M1; m++) {
-    // Step 2' on the tensor cores once the operand tile is in: D2 = A2 * C2^T.
-    if (!__syncthreads_and(tc::mbar_wait(&bar[0], phase, kWaitNs))) {
+    // The operand tile of row m arrives by bulk copy (issued while the
+    // previous row's overlap-add ran).
+    if (!__syncthreads_and(tc::mbar_wait(&bar[0], st.phase, kWaitNs))) {
       if (tid == 0) atomicOr(sa.err, kErrWaitTile);
       break;
     }
-    if (tid == 0) {
-      tc::fence_after_sync();
-      constexpr uint32_t id2 = tc::idesc_f16(128, C::N2);
-      const uint32_t sbo_b = (C::K2 / 8) * 128;
-      const uint32_t d = tmem + C::D2_COL;
-      for (int ks = 0; ks < C::K2 / 16; ks++) {
-        const uint64_t ah = tc::sdesc(sbase + S::A2 + ks * 32, 16, 1024, tc::LAYOUT_SW128);
-        const uint64_t al = tc::sdesc(sbase + S::A2 + C::A2_BYTES + ks * 32, 16, 1024, tc::LAYOUT_SW128);
-        const uint64_t bh = tc::sdesc(sbase + S::C2 + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
-        const uint64_t bl = tc::sdesc(sbase + S::C2 + C::B2_BYTES + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
-        tc::mma_f16(d, ah, bh, id2, ks > 0);
-        tc::mma_f16(d, ah, bl, id2, 1);
-        tc::mma_f16(d, al, bh, id2, 1);
+    // A1 (the operand tile's space) is consumed once step 1' is done: the
+    // next row's tile starts moving in while the overlap-add runs.
+    const bool ok = inverse_row<N>(sa, st, m, M0, M1, seg, J0, ncell, [&] {
+      if (tid == 0 && m + 1 < M1) {
+        tc::mbar_expect_tx(&bar[0], S::TILE);
+        tc::bulk_load(sm + S::A2, tile_of(m + 1), S::TILE, &bar[0]);
       }
-      tc::mma_commit(&bar[1]);
-    }
-    if (!__syncthreads_and(tc::mbar_wait(&bar[1], phase, kWaitNs))) {
-      if (tid == 0) atomicOr(sa.err, kErrWaitColumn);
-      break;
-    }
-    tc::fence_after_sync();
-
-    // V. Row-inverse operand: tile = parity of the block column, row (y, slot).
-    {
-      const int s = warp & 3, h = warp >> 2;
-      const int r2 = 32 * s + lane;
-      const int kp = r2 >> 3, bl = r2 & 7;
-      const int tile = (J0 + bl) & 1, slot = bl >> 1;
-      uint8_t* t0 = sm + S::A1 + tile * S::A1_STRIDE;
-      float v[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + 32 * h, v);
-#pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int y = 16 * h + j;
-        uint32_t hi, lo;
-        tc::split_pair(v[2 * j], v[2 * j + 1], hi, lo);
-        const uint32_t o = tc::off_il(4 * y + slot, 2 * kp, C::K1);
-        *reinterpret_cast<uint32_t*>(t0 + o) = hi;
-        *reinterpret_cast<uint32_t*>(t0 + C::A1_BYTES + o) = lo;
-      }
-    }
-    tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-
-    // Step 1' on the tensor cores: D1[tile] = A1[tile] * C1(tile)^T.
-    if (tid == 0) {
-      tc::fence_after_sync();
-      constexpr uint32_t id1 = tc::idesc_f16(128, C::N1);
-      const uint32_t sbo = (C::K1 / 8) * 128;
-      for (int t = 0; t < C::T1; t++) {
-        const uint32_t a_hi = sbase + S::A1 + t * S::A1_STRIDE, a_lo = a_hi + C::A1_BYTES;
-        const uint32_t b_hi = sbase + S::C1 + t * 2 * C::B1_BYTES, b_lo = b_hi + C::B1_BYTES;
-        const uint32_t d = tmem + C::D1_COL + t * C::N1;
-        for (int ks = 0; ks < C::K1 / 16; ks++) {
-          const uint64_t ah = tc::sdesc(a_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
-          const uint64_t al = tc::sdesc(a_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
-          const uint64_t bh = tc::sdesc(b_hi + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
-          const uint64_t bl = tc::sdesc(b_lo + ks * 256, 128, sbo, tc::LAYOUT_INTERLEAVE);
-          tc::mma_f16(d, ah, bh, id1, ks > 0);
-          tc::mma_f16(d, ah, bl, id1, 1);
-          tc::mma_f16(d, al, bh, id1, 1);
-        }
-      }
-      tc::mma_commit(&bar[2]);
-    }
-    if (!__syncthreads_and(tc::mbar_wait(&bar[2], phase, kWaitNs))) {
-      if (tid == 0) atomicOr(sa.err, kErrWaitRow);
-      break;
-    }
-    phase ^= 1;
-    tc::fence_after_sync();
-    // A1 (the operand tile's space) is consumed: the next row's tile starts
-    // moving in while the overlap-add runs.
-    if (tid == 0 && m + 1 < M1) {
-      tc::mbar_expect_tx(&bar[0], S::TILE);
-      tc::bulk_load(sm + S::A2, tile_of(m + 1), S::TILE, &bar[0]);
-    }
-
-    // O. Overlap-add. Thread: block row y of block bl; y < n/2 finishes cell
-    // row m-1 (P_old), y >= n/2 starts cell row m (P_new).
-    {
-      const int t = warp >> 2, s = warp & 3;
-      const int r = 32 * s + lane;
-      const int y = r >> 2, slot = r & 3;
-      const int bl = 2 * slot + ((t ^ J0) & 1);
-      float v[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
-#pragma unroll
-      for (int x = 0; x < 32; x++) v[x] *= out_scale<N>();
-      const bool top = y < S::CH;
-      const int yy = top ? y : y - S::CH;
-      const bool right_ok = bl < ncell;                // right half -> cell bl
-      const bool left_ok = bl >= 1 && bl - 1 < ncell;  // left half -> cell bl-1
-      const bool seam_top = m == M0;                   // cell row m-1 is another segment's (or none)
-      if (top) {
-        if (seam_top) {
-          if (M0 > 0 && right_ok) {
-            float* t0 = sa.seam_t + ((size_t)((seg - 1) * 2) * S::CH + yy) * sa.seam_w + (J0 + bl) * S::CW;
-#pragma unroll
-            for (int x = 0; x < S::CW; x += 4)
-              *reinterpret_cast<float4*>(t0 + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
-          }
-        } else if (right_ok) {
-          float* p = P_old + bl * S::PC + yy * S::PR;
-#pragma unroll
-          for (int x = 0; x < S::CW; x += 4) {
-            float4 q = *reinterpret_cast<float4*>(p + x);
-            q.x += v[16 + x], q.y += v[17 + x], q.z += v[18 + x], q.w += v[19 + x];
-            *reinterpret_cast<float4*>(p + x) = q;
-          }
-        }
-      } else if (right_ok) {
-        float* p = P_new + bl * S::PC + yy * S::PR;
-#pragma unroll
-        for (int x = 0; x < S::CW; x += 4)
-          *reinterpret_cast<float4*>(p + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
-      }
-      __syncthreads();
-      if (top) {
-        if (seam_top) {
-          if (M0 > 0 && left_ok) {
-            float* t1 = sa.seam_t + ((size_t)((seg - 1) * 2 + 1) * S::CH + yy) * sa.seam_w + (J0 + bl - 1) * S::CW;
-#pragma unroll
-            for (int x = 0; x < S::CW; x += 4)
-              *reinterpret_cast<float4*>(t1 + x) = make_float4(v[x], v[x + 1], v[x + 2], v[x + 3]);
-          }
-        } else if (left_ok) {
-          const float* p = P_old + (bl - 1) * S::PC + yy * S::PR;
-          float o[16];
-#pragma unroll
-          for (int x = 0; x < S::CW; x += 4) {
-            const float4 q = *reinterpret_cast<const float4*>(p + x);
-            o[x] = q.x + v[x], o[x + 1] = q.y + v[x + 1], o[x + 2] = q.z + v[x + 2], o[x + 3] = q.w + v[x + 3];
-          }
-          emit16(sa, (m - 1) * S::CH + yy, (J0 + bl - 1) * S::CW, o);
-        }
-      } else if (left_ok) {
-        float* p = P_new + (bl - 1) * S::PC + yy * S::PR;
-        const bool seam_bot = m == M1 - 1 && seg < sa.segs - 1;
-        float* sb = sa.seam_b + ((size_t)seg * S::CH + yy) * sa.seam_w + (J0 + bl - 1) * S::CW;
-#pragma unroll
-        for (int x = 0; x < S::CW; x += 4) {
-          float4 q = *reinterpret_cast<float4*>(p + x);
-          q.x += v[x], q.y += v[x + 1], q.z += v[x + 2], q.w += v[x + 3];
-          if (seam_bot) *reinterpret_cast<float4*>(sb + x) = q;
-          else *reinterpret_cast<float4*>(p + x) = q;
-        }
-      }
-    }
-    float* tmp = P_old;
-    P_old = P_new;
-    P_new = tmp;
-    tc::fence_before_sync();
-    __syncthreads();
+    });
+    if (!ok) break;
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
+  if (warp == 0) tc::tmem_dealloc(st.tmem, C::TMEM_COLS);
 }
 
 template <class K>
@@ -1119,6 +1184,9 @@ cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& 
   const int bm = planes[0].inv.bm;
   int maxw = 0;
   for (int i = 0; i < n; i++) maxw = std::max(maxw, planes[i].inv.g.W);
+  constexpr size_t smem = SwpCfg<32>::BYTES;
+  static_assert(kTcSweepCtasPerSm * (SwpCfg<32>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
+  static_assert(SwpCfg<32>::TJ == kTcSweepCells, "cells per strip");
   // Filter: one CTA per (row, strip) group of every plane.
   cudaError_t e = t.filter_minb == 3   ? launch_filter<3>(Bf, bm, st)
                   : t.filter_minb == 4 ? launch_filter<4>(Bf, bm, st)
@@ -1126,9 +1194,6 @@ cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& 
   if (e != cudaSuccess) return e;
   if (mark) cudaEventRecord(mark, st);
   // Inverse + overlap-add: one CTA per (strip, segment) of every plane.
-  constexpr size_t smem = SwpCfg<32>::BYTES;
-  static_assert(kTcSweepCtasPerSm * (SwpCfg<32>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
-  static_assert(SwpCfg<32>::TJ == kTcSweepCells, "cells per strip");
   e = prepare(k_sweep_tc<32>, smem);
   if (e != cudaSuccess) return e;
   k_sweep_tc<32><<<B.cta0[n], kTcThreads, smem, st>>>(B);
