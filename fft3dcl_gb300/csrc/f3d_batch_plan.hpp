@@ -9,9 +9,9 @@
 
 namespace f3d {
 
-// Blocks per tensor-core forward group (one M = 128 tile of 8 blocks x 16
-// packed columns).
-constexpr int kTcGroupBlocks = 8;
+// Blocks per tensor-core forward group: one M = 128 tile of blocks x n/2
+// packed columns (8 blocks of 32 x 32, 16 of 16 x 16).
+constexpr int tc_group_size(int bw) { return 256 / bw; }
 
 // The forward batch parameter of `planes` (false: not one batch).
 inline bool forward_batch(const TcFwdArgs* planes, int n, TcFwdBatch& B) {
@@ -20,9 +20,12 @@ inline bool forward_batch(const TcFwdArgs* planes, int n, TcFwdBatch& B) {
   B.n = n;
   for (int i = 0; i < n; i++) {
     const TcFwdArgs& a = planes[i];
-    if (a.g.bw != 32 || a.g.bh != 32 || a.g.mode != 1 || a.fmt != planes[0].fmt) return false;
+    if ((a.g.bw != 16 && a.g.bw != 32) || a.g.bh != a.g.bw || a.g.bw != planes[0].g.bw || a.g.mode != 1 ||
+        a.fmt != planes[0].fmt)
+      return false;
     B.p[i] = a;
-    B.grp0[i + 1] = B.grp0[i] + (a.g.nb + kTcGroupBlocks - 1) / kTcGroupBlocks;
+    const int gs = tc_group_size(a.g.bw);
+    B.grp0[i + 1] = B.grp0[i] + (a.g.nb + gs - 1) / gs;
   }
   for (int i = n + 1; i <= kMaxBatch; i++) B.grp0[i] = B.grp0[n];
   return true;
@@ -36,8 +39,8 @@ inline bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepB
   B.n = n;
   for (int i = 0; i < n; i++) {
     const SweepArgs& a = planes[i];
-    if (a.inv.g.bw != 32 || a.inv.g.bh != 32 || !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm ||
-        a.inv.half != planes[0].inv.half)
+    if ((a.inv.g.bw != 16 && a.inv.g.bw != 32) || a.inv.g.bh != a.inv.g.bw || a.inv.g.bw != planes[0].inv.g.bw ||
+        !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm || a.inv.half != planes[0].inv.half)
       return false;
     B.p[i] = a;
   }

@@ -74,7 +74,7 @@ static bool pow2_in(int v, int lo, int hi) { return v >= lo && v <= hi && (v & (
 bool form_supported(int form, int bw, int bh) {
   if (form == F3D_FORM_EXACT) return pow2_in(bw, 4, 512) && pow2_in(bh, 4, 512);
   if (form == F3D_FORM_FAST) return pow2_in(bw, 8, 64) && pow2_in(bh, 8, 64);
-  if (form == F3D_FORM_TC) return bw == 32 && bh == 32;
+  if (form == F3D_FORM_TC) return bw == bh && (bw == 16 || bw == 32);
   return false;
 }
 

@@ -219,7 +219,7 @@ bool sweep_supported(int form, const Geo& g, int bm) {
 }
 
 void sweep_plan(int form, const Geo& g, int sm_count, int* strips, int* segs) {
-  const int tj = form == F3D_FORM_TC ? kTcSweepCells : kSweepThreads / g.bw - 1;
+  const int tj = form == F3D_FORM_TC ? tc_sweep_cells(g.bw) : kSweepThreads / g.bw - 1;
   const int per_sm = form == F3D_FORM_TC ? kTcSweepCtasPerSm : F3D_SWEEP_MINB;
   const int cells_x = (g.W + g.bw / 2 - 1) / (g.bw / 2);
   const int cells_y = (g.H + g.bh / 2 - 1) / (g.bh / 2);

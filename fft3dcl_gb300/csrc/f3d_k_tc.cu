@@ -72,9 +72,23 @@ struct TcCfg {
   static constexpr uint32_t B1_BYTES = N1 * K1 * 2, B2_BYTES = N2 * K2 * 2;
   static constexpr uint32_t TMEM_COLS = 128;
   static constexpr uint32_t D1_COL = 0, D2_COL = 64;
-  static_assert(N == 32, "the tensor-core form is built for 32 x 32 blocks");
+  static_assert(N == 16 || N == 32, "the tensor-core form is built for 16 x 16 and 32 x 32 blocks");
   static_assert(T1 * N1 <= (int)D2_COL && D2_COL + N2 <= (int)TMEM_COLS, "tensor memory columns");
 };
+
+// The step-2 operand (128 rows, K2 = 2N fp16 columns; the column inverse's
+// operand tile too): SWIZZLE_128B for N = 32 (rows of 128 bytes), the
+// interleaved core-matrix layout for N = 16 (rows of 64 bytes).
+template <int N>
+__host__ __device__ constexpr uint32_t a2_off(int row, int k) {
+  return N == 32 ? tc::off_sw128(row, k) : tc::off_il(row, k, 2 * N);
+}
+// Descriptor of K-step ks (16 columns) of a step-2 operand at base.
+template <int N>
+__device__ __forceinline__ uint64_t a2_desc(uint32_t base, int ks) {
+  if constexpr (N == 32) return tc::sdesc(base + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+  else return tc::sdesc(base + ks * 256, 128, (2 * N / 8) * 128, tc::LAYOUT_INTERLEAVE);
+}
 
 constexpr int kTcThreads = 256;
 // Filter-kernel variants: CTAs per SM (minb) and filter_batch(minb), the
@@ -314,13 +328,13 @@ __global__ void __launch_bounds__(kTcThreads, kFwdMaxCtasPerSm) k_forward_tc(con
       const int t = warp >> 2, s = warp & 3;
       const int r1 = 32 * s + lane;
       const int bl = t * C::BPT1 + r1 / N, y = r1 % N;
-      float v[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
+      float v[C::N1];
+      tc::tmem_ld<C::N1>(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
 #pragma unroll
       for (int kp = 0; kp < C::NY; kp++) {
         uint32_t hi, lo;
         tc::split_pair(v[2 * kp], v[2 * kp + 1], hi, lo);
-        const uint32_t o = tc::off_sw128(bl * C::NY + kp, 2 * y);
+        const uint32_t o = a2_off<N>(bl * C::NY + kp, 2 * y);
         *reinterpret_cast<uint32_t*>(sm + L::A2 + o) = hi;
         *reinterpret_cast<uint32_t*>(sm + L::A2 + C::A2_BYTES + o) = lo;
       }
@@ -336,8 +350,8 @@ __global__ void __launch_bounds__(kTcThreads, kFwdMaxCtasPerSm) k_forward_tc(con
       const uint32_t sbo_b = (C::K2 / 8) * 128;
       const uint32_t d = tmem + C::D2_COL;
       for (int ks = 0; ks < C::K2 / 16; ks++) {
-        const uint64_t ah = tc::sdesc(sbase + L::A2 + ks * 32, 16, 1024, tc::LAYOUT_SW128);
-        const uint64_t al = tc::sdesc(sbase + L::A2 + C::A2_BYTES + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+        const uint64_t ah = a2_desc<N>(sbase + L::A2, ks);
+        const uint64_t al = a2_desc<N>(sbase + L::A2 + C::A2_BYTES, ks);
         const uint64_t bh = tc::sdesc(sbase + L::B2 + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
         const uint64_t bl = tc::sdesc(sbase + L::B2 + C::B2_BYTES + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
         tc::mma_f16(d, ah, bh, id2, ks > 0);
@@ -363,12 +377,12 @@ __global__ void __launch_bounds__(kTcThreads, kFwdMaxCtasPerSm) k_forward_tc(con
       const int s = warp & 3, h = warp >> 2;
       const int r2 = 32 * s + lane;
       const int bl = r2 / C::NY, kp = r2 % C::NY;
-      float v[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + 32 * h, v);
+      float v[N];  // half of the N2 = 2N columns: NY values of ky, (re, im)
+      tc::tmem_ld<N>(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + N * h, v);
       float2* o = stage + bl * C::PS + kp;
 #pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int ky = 16 * h + j;
+      for (int j = 0; j < C::NY; j++) {
+        const int ky = C::NY * h + j;
         o[ky * C::FBW] = make_float2(v[2 * j] * a.out_scale, v[2 * j + 1] * a.out_scale);
       }
     }
@@ -380,7 +394,7 @@ __global__ void __launch_bounds__(kTcThreads, kFwdMaxCtasPerSm) k_forward_tc(con
       float2* blk = stage + bl * C::PS;
       const float2 P = blk[ky * C::FBW], Q = blk[((N - ky) % N) * C::FBW];
       __syncwarp();
-      // Both halves of a pair (ky, n-ky) sit in the same warp for N = 32.
+      // Both halves of a pair (ky, n-ky) sit in the same warp (N <= 32).
       blk[ky * C::FBW] = make_float2(0.5f * (P.x + Q.x), 0.5f * (P.y - Q.y));
       blk[ky * C::FBW + C::NY] = make_float2(0.5f * (P.y + Q.y), 0.5f * (Q.x - P.x));
       if (a.chroma_norm != 0.0f) {
@@ -498,34 +512,38 @@ __host__ __device__ constexpr float out_scale() {
   return 1.0f / (kInvPre * N * N);
 }
 
-// Packs and stores samples x0.. x0+15 of plane row y (bounds-checked), with
-// 16-byte stores where the run is inside the plane and aligned.
-__device__ __forceinline__ void emit16(const SweepArgs& sa, int y, int x0, const float (&v)[16]) {
+// Packs and stores samples x0 .. x0+W-1 (W = 8 or 16) of plane row y
+// (bounds-checked), with 8- and 16-byte stores where the run is inside the
+// plane and aligned.
+template <int W>
+__device__ __forceinline__ void emit_run(const SweepArgs& sa, int y, int x0, const float (&v)[W]) {
+  static_assert(W == 8 || W == 16, "run width");
   if (y >= sa.inv.g.H) return;
   uint8_t* row = sa.dst + (long long)y * sa.pitch;
-  const bool full = x0 + 16 <= sa.inv.g.W;
+  const bool full = x0 + W <= sa.inv.g.W;
   if (full && sa.fmt == FMT_U16 && ((reinterpret_cast<uintptr_t>(row) + 2 * x0) & 15) == 0) {
-    uint32_t w[8];
+    uint32_t w[W / 2];
 #pragma unroll
-    for (int k = 0; k < 8; k++)
+    for (int k = 0; k < W / 2; k++)
       w[k] = pack_u16(v[2 * k] + sa.chroma_norm, sa.inv_norm, sa.max_pix) |
              (pack_u16(v[2 * k + 1] + sa.chroma_norm, sa.inv_norm, sa.max_pix) << 16);
     uint4* p = reinterpret_cast<uint4*>(row + 2 * x0);
-    p[0] = make_uint4(w[0], w[1], w[2], w[3]);
-    p[1] = make_uint4(w[4], w[5], w[6], w[7]);
+#pragma unroll
+    for (int k = 0; k < W / 8; k++) p[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
     return;
   }
-  if (full && sa.fmt == FMT_U8 && ((reinterpret_cast<uintptr_t>(row) + x0) & 15) == 0) {
-    uint32_t w[4];
+  if (full && sa.fmt == FMT_U8 && ((reinterpret_cast<uintptr_t>(row) + x0) & (W - 1)) == 0) {
+    uint32_t w[W / 4];
 #pragma unroll
-    for (int k = 0; k < 4; k++)
+    for (int k = 0; k < W / 4; k++)
       w[k] = pack_u8(v[4 * k] + sa.chroma_norm) | (pack_u8(v[4 * k + 1] + sa.chroma_norm) << 8) |
              (pack_u8(v[4 * k + 2] + sa.chroma_norm) << 16) | (pack_u8(v[4 * k + 3] + sa.chroma_norm) << 24);
-    *reinterpret_cast<uint4*>(row + x0) = make_uint4(w[0], w[1], w[2], w[3]);
+    if constexpr (W == 16) *reinterpret_cast<uint4*>(row + x0) = make_uint4(w[0], w[1], w[2], w[3]);
+    else *reinterpret_cast<uint2*>(row + x0) = make_uint2(w[0], w[1]);
     return;
   }
 #pragma unroll
-  for (int k = 0; k < 16; k++) {
+  for (int k = 0; k < W; k++) {
     if (x0 + k >= sa.inv.g.W) break;
     float s = v[k];
     if (sa.chroma_norm != 0.0f) s += sa.chroma_norm;
@@ -551,7 +569,7 @@ __device__ __forceinline__ void tile_rows(uint8_t* img, uint8_t* prev, bool skip
   using C = TcCfg<N>;
   using S = SwpCfg<N>;
   const int r2 = tid & 127, h = tid >> 7;
-  const int kp = r2 >> 3, bl = r2 & 7;
+  const int kp = r2 / C::G, bl = r2 % C::G;
   if (bl == C::G - 1 && skip_last) return;
   const float2* fb = fbuf + bl * S::FS;
 #pragma unroll
@@ -573,11 +591,11 @@ __device__ __forceinline__ void tile_rows(uint8_t* img, uint8_t* prev, bool skip
       }
       tc::split_pair(z.x * kInvPre, z.y * kInvPre, hi[u], lo[u]);
     }
-    const uint32_t o = tc::off_sw128(r2, 2 * (C::NY * h + 4 * cq));
+    const uint32_t o = a2_off<N>(r2, 2 * (C::NY * h + 4 * cq));
     *reinterpret_cast<uint4*>(img + o) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
     *reinterpret_cast<uint4*>(img + C::A2_BYTES + o) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
     if (bl == 0 && prev) {
-      const uint32_t op = tc::off_sw128(r2 + C::G - 1, 2 * (C::NY * h + 4 * cq));
+      const uint32_t op = a2_off<N>(r2 + C::G - 1, 2 * (C::NY * h + 4 * cq));
       *reinterpret_cast<uint4*>(prev + op) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
       *reinterpret_cast<uint4*>(prev + C::A2_BYTES + op) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
     }
@@ -748,8 +766,8 @@ __device__ __forceinline__ bool inverse_row(const SweepArgs& sa, InvState& st, i
     const uint32_t sbo_b = (C::K2 / 8) * 128;
     const uint32_t d = tmem + C::D2_COL;
     for (int ks = 0; ks < C::K2 / 16; ks++) {
-      const uint64_t ah = tc::sdesc(sbase + S::A2 + ks * 32, 16, 1024, tc::LAYOUT_SW128);
-      const uint64_t al = tc::sdesc(sbase + S::A2 + C::A2_BYTES + ks * 32, 16, 1024, tc::LAYOUT_SW128);
+      const uint64_t ah = a2_desc<N>(sbase + S::A2, ks);
+      const uint64_t al = a2_desc<N>(sbase + S::A2 + C::A2_BYTES, ks);
       const uint64_t bh = tc::sdesc(sbase + S::C2 + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
       const uint64_t bl = tc::sdesc(sbase + S::C2 + C::B2_BYTES + ks * 256, 128, sbo_b, tc::LAYOUT_INTERLEAVE);
       tc::mma_f16(d, ah, bh, id2, ks > 0);
@@ -768,17 +786,17 @@ __device__ __forceinline__ bool inverse_row(const SweepArgs& sa, InvState& st, i
   {
     const int s = warp & 3, h = warp >> 2;
     const int r2 = 32 * s + lane;
-    const int kp = r2 >> 3, bl = r2 & 7;
+    const int kp = r2 / C::G, bl = r2 % C::G;
     const int tile = (J0 + bl) & 1, slot = bl >> 1;
     uint8_t* t0 = sm + S::A1 + tile * S::A1_STRIDE;
-    float v[32];
-    tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + 32 * h, v);
+    float v[N];  // half of the N2 = 2N columns: NY values of y, (re, im)
+    tc::tmem_ld<N>(tmem + ((uint32_t)(32 * s) << 16) + C::D2_COL + N * h, v);
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
-      const int y = 16 * h + j;
+    for (int j = 0; j < C::NY; j++) {
+      const int y = C::NY * h + j;
       uint32_t hi, lo;
       tc::split_pair(v[2 * j], v[2 * j + 1], hi, lo);
-      const uint32_t o = tc::off_il(4 * y + slot, 2 * kp, C::K1);
+      const uint32_t o = tc::off_il((C::G / 2) * y + slot, 2 * kp, C::K1);
       *reinterpret_cast<uint32_t*>(t0 + o) = hi;
       *reinterpret_cast<uint32_t*>(t0 + C::A1_BYTES + o) = lo;
     }
@@ -823,12 +841,12 @@ __device__ __forceinline__ bool inverse_row(const SweepArgs& sa, InvState& st, i
   {
     const int t = warp >> 2, s = warp & 3;
     const int r = 32 * s + lane;
-    const int y = r >> 2, slot = r & 3;
+    const int y = r / (C::G / 2), slot = r % (C::G / 2);
     const int bl = 2 * slot + ((t ^ J0) & 1);
-    float v[32];
-    tc::tmem_ld32(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
+    float v[N];
+    tc::tmem_ld<N>(tmem + ((uint32_t)(32 * s) << 16) + C::D1_COL + t * C::N1, v);
 #pragma unroll
-    for (int x = 0; x < 32; x++) v[x] *= out_scale<N>();
+    for (int x = 0; x < N; x++) v[x] *= out_scale<N>();
     const bool top = y < S::CH;
     const int yy = top ? y : y - S::CH;
     const bool right_ok = bl < ncell;                // right half -> cell bl
@@ -840,14 +858,14 @@ __device__ __forceinline__ bool inverse_row(const SweepArgs& sa, InvState& st, i
           float* t0 = sa.seam_t + ((size_t)((seg - 1) * 2) * S::CH + yy) * sa.seam_w + (J0 + bl) * S::CW;
 #pragma unroll
           for (int x = 0; x < S::CW; x += 4)
-            *reinterpret_cast<float4*>(t0 + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
+            *reinterpret_cast<float4*>(t0 + x) = make_float4(v[S::CW + x], v[S::CW + x + 1], v[S::CW + x + 2], v[S::CW + x + 3]);
         }
       } else if (right_ok) {
         float* p = P_old + bl * S::PC + yy * S::PR;
 #pragma unroll
         for (int x = 0; x < S::CW; x += 4) {
           float4 q = *reinterpret_cast<float4*>(p + x);
-          q.x += v[16 + x], q.y += v[17 + x], q.z += v[18 + x], q.w += v[19 + x];
+          q.x += v[S::CW + x], q.y += v[S::CW + x + 1], q.z += v[S::CW + x + 2], q.w += v[S::CW + x + 3];
           *reinterpret_cast<float4*>(p + x) = q;
         }
       }
@@ -855,7 +873,7 @@ __device__ __forceinline__ bool inverse_row(const SweepArgs& sa, InvState& st, i
       float* p = P_new + bl * S::PC + yy * S::PR;
 #pragma unroll
       for (int x = 0; x < S::CW; x += 4)
-        *reinterpret_cast<float4*>(p + x) = make_float4(v[16 + x], v[17 + x], v[18 + x], v[19 + x]);
+        *reinterpret_cast<float4*>(p + x) = make_float4(v[S::CW + x], v[S::CW + x + 1], v[S::CW + x + 2], v[S::CW + x + 3]);
     }
     __syncthreads();
     if (top) {
@@ -868,13 +886,13 @@ __device__ __forceinline__ bool inverse_row(const SweepArgs& sa, InvState& st, i
         }
       } else if (left_ok) {
         const float* p = P_old + (bl - 1) * S::PC + yy * S::PR;
-        float o[16];
+        float o[S::CW];
 #pragma unroll
         for (int x = 0; x < S::CW; x += 4) {
           const float4 q = *reinterpret_cast<const float4*>(p + x);
           o[x] = q.x + v[x], o[x + 1] = q.y + v[x + 1], o[x + 2] = q.z + v[x + 2], o[x + 3] = q.w + v[x + 3];
         }
-        emit16(sa, (m - 1) * S::CH + yy, (J0 + bl - 1) * S::CW, o);
+        emit_run<S::CW>(sa, (m - 1) * S::CH + yy, (J0 + bl - 1) * S::CW, o);
       }
     } else if (left_ok) {
       float* p = P_new + (bl - 1) * S::PC + yy * S::PR;
@@ -1084,9 +1102,14 @@ std::vector<uint8_t> tables_n(const std::vector<double>& wx, const std::vector<d
 
 }  // namespace
 
-bool tc_supported(int mode, int bw, int bh, int bm) { return mode == 1 && bw == 32 && bh == 32 && bm != 0; }
+bool tc_supported(int mode, int bw, int bh, int bm) {
+  return mode == 1 && bw == bh && (bw == 16 || bw == 32) && bm != 0;
+}
 
-static_assert(TcCfg<32>::G == kTcGroupBlocks, "forward group size of the batch plan");
+int tc_group_blocks(int n) { return 128 / (n / 2); }
+int tc_sweep_cells(int n) { return tc_group_blocks(n) - 1; }
+
+static_assert(TcCfg<32>::G == 8 && TcCfg<16>::G == 16, "forward group sizes of the batch plan");
 
 std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::vector<double>& wy,
                                const std::vector<double>& sxa, const std::vector<double>& sxb,
@@ -1094,41 +1117,52 @@ std::vector<uint8_t> tc_tables(int n, const std::vector<double>& wx, const std::
   for (const auto* v : {&wx, &wy, &sxa, &sxb, &sy})
     if ((int)v->size() != n) return {};
   if (n == 32) return tables_n<32>(wx, wy, sxa, sxb, sy);
+  if (n == 16) return tables_n<16>(wx, wy, sxa, sxb, sy);
   return {};
 }
 
-cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st) {
-  TcFwdBatch B;
-  if (!forward_batch(planes, n, B)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
+namespace {
+
+template <int N>
+cudaError_t launch_forward_n(const TcFwdBatch& B, const TcFwdArgs* planes, int n, const TcTune& t,
+                             cudaStream_t st) {
   // The split kernel (hi + lo step-1 operand) also takes planes that need no
   // split; it fits two CTAs per SM, the other three.
   bool split = false;
   for (int i = 0; i < n; i++) split = split || planes[i].split;
   const int fmt = planes[0].fmt;
   if (fmt == FMT_U8 && split) return cudaErrorNotSupported;
-  auto k = fmt == FMT_U8 ? k_forward_tc<32, 1, false>
-           : fmt == FMT_U16 ? (split ? k_forward_tc<32, 2, true> : k_forward_tc<32, 2, false>)
-                            : k_forward_tc<32, 4, true>;
-  const size_t smem = split ? FwdSmem<32, true>::BYTES : FwdSmem<32, false>::BYTES;
+  auto k = fmt == FMT_U8 ? k_forward_tc<N, 1, false>
+           : fmt == FMT_U16 ? (split ? k_forward_tc<N, 2, true> : k_forward_tc<N, 2, false>)
+                            : k_forward_tc<N, 4, true>;
+  const size_t smem = split ? FwdSmem<N, true>::BYTES : FwdSmem<N, false>::BYTES;
   cudaError_t attr = prepare(k, smem);
   if (attr != cudaSuccess) return attr;
   const int ngroups = B.grp0[n];
   if (ngroups == 0) return cudaSuccess;
   const int per_sm = std::max(1, std::min(t.fwd_ctas_per_sm, split ? 2 : kFwdMaxCtasPerSm));
-  static_assert(kFwdMaxCtasPerSm * (FwdSmem<32, false>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
-  static_assert(2 * (FwdSmem<32, true>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
+  static_assert(kFwdMaxCtasPerSm * (FwdSmem<N, false>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
+  static_assert(2 * (FwdSmem<N, true>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
   const int grid = std::min(ngroups, per_sm * sm_count());
   k<<<grid, kTcThreads, smem, st>>>(B);
   count_launch();
   return cudaGetLastError();
 }
 
+}  // namespace
+
+cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st) {
+  TcFwdBatch B;
+  if (!forward_batch(planes, n, B)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
+  return planes[0].g.bw == 16 ? launch_forward_n<16>(B, planes, n, t, st) : launch_forward_n<32>(B, planes, n, t, st);
+}
+
 cudaError_t launch_forward_tc(const TcFwdArgs& a, cudaStream_t st) { return launch_forward_tc_batch(&a, 1, TcTune{}, st); }
 
-template <int BM, int MINB, bool HALF>
+template <int N, int BM, int MINB, bool HALF>
 cudaError_t launch_filter_bm(const SweepBatch& B, cudaStream_t st) {
-  constexpr size_t smem = SwpCfg<32>::F_BYTES;
-  auto k = k_filter_tc<32, BM, MINB, HALF>;
+  constexpr size_t smem = SwpCfg<N>::F_BYTES;
+  auto k = k_filter_tc<N, BM, MINB, HALF>;
   cudaError_t e = prepare(k, smem);
   if (e != cudaSuccess) return e;
   if (B.cta0[B.n] == 0) return cudaSuccess;
@@ -1137,22 +1171,22 @@ cudaError_t launch_filter_bm(const SweepBatch& B, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int MINB, bool HALF>
+template <int N, int MINB, bool HALF>
 cudaError_t launch_filter_h(const SweepBatch& B, int bm, cudaStream_t st) {
   switch (bm) {
-  case -1: return launch_filter_bm<-1, MINB, HALF>(B, st);
-  case 1: return launch_filter_bm<1, MINB, HALF>(B, st);
-  case 2: return launch_filter_bm<2, MINB, HALF>(B, st);
-  case 3: return launch_filter_bm<3, MINB, HALF>(B, st);
-  case 4: return launch_filter_bm<4, MINB, HALF>(B, st);
+  case -1: return launch_filter_bm<N, -1, MINB, HALF>(B, st);
+  case 1: return launch_filter_bm<N, 1, MINB, HALF>(B, st);
+  case 2: return launch_filter_bm<N, 2, MINB, HALF>(B, st);
+  case 3: return launch_filter_bm<N, 3, MINB, HALF>(B, st);
+  case 4: return launch_filter_bm<N, 4, MINB, HALF>(B, st);
   default: return cudaErrorNotSupported;
   }
 }
 
 // The planes of a batch store their spectra alike, fp32 or fp16 (sweep_batches checks).
-template <int MINB>
+template <int N, int MINB>
 cudaError_t launch_filter(const SweepBatch& B, int bm, cudaStream_t st) {
-  return B.p[0].inv.half ? launch_filter_h<MINB, true>(B, bm, st) : launch_filter_h<MINB, false>(B, bm, st);
+  return B.p[0].inv.half ? launch_filter_h<N, MINB, true>(B, bm, st) : launch_filter_h<N, MINB, false>(B, bm, st);
 }
 
 // Finishes the seam cell rows of every plane of the batch: blockIdx.z runs
@@ -1177,35 +1211,47 @@ __global__ void __launch_bounds__(256) k_seam_merge_batch(const __grid_constant_
   store_sample(sa.dst + (long long)y * sa.pitch, x, v, sa.fmt, sa.inv_norm, sa.max_pix);
 }
 
-cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
-                                  cudaEvent_t mark) {
-  SweepBatch Bf, B, Bm;
-  if (!sweep_batches(planes, n, Bf, B, Bm)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
-  const int bm = planes[0].inv.bm;
-  int maxw = 0;
-  for (int i = 0; i < n; i++) maxw = std::max(maxw, planes[i].inv.g.W);
-  constexpr size_t smem = SwpCfg<32>::BYTES;
-  static_assert(kTcSweepCtasPerSm * (SwpCfg<32>::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
-  static_assert(SwpCfg<32>::TJ == kTcSweepCells, "cells per strip");
+namespace {
+
+template <int N>
+cudaError_t launch_sweep_n(const SweepBatch& Bf, const SweepBatch& B, const SweepBatch& Bm, int n, int maxw,
+                           const TcTune& t, cudaStream_t st, cudaEvent_t mark) {
+  using S = SwpCfg<N>;
+  const int bm = B.p[0].inv.bm;
+  constexpr size_t smem = S::BYTES;
+  static_assert(kTcSweepCtasPerSm * (S::BYTES + 1024) <= 228 * 1024, "CTAs per SM");
   // Filter: one CTA per (row, strip) group of every plane.
-  cudaError_t e = t.filter_minb == 3   ? launch_filter<3>(Bf, bm, st)
-                  : t.filter_minb == 4 ? launch_filter<4>(Bf, bm, st)
-                                       : launch_filter<5>(Bf, bm, st);
+  cudaError_t e = t.filter_minb == 3   ? launch_filter<N, 3>(Bf, bm, st)
+                  : t.filter_minb == 4 ? launch_filter<N, 4>(Bf, bm, st)
+                                       : launch_filter<N, 5>(Bf, bm, st);
   if (e != cudaSuccess) return e;
   if (mark) cudaEventRecord(mark, st);
   // Inverse + overlap-add: one CTA per (strip, segment) of every plane.
-  e = prepare(k_sweep_tc<32>, smem);
+  e = prepare(k_sweep_tc<N>, smem);
   if (e != cudaSuccess) return e;
-  k_sweep_tc<32><<<B.cta0[n], kTcThreads, smem, st>>>(B);
+  k_sweep_tc<N><<<B.cta0[n], kTcThreads, smem, st>>>(B);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // Seam rows of all planes.
   if (Bm.cta0[n] == 0) return cudaSuccess;
-  dim3 grid((maxw + 255) / 256, SwpCfg<32>::CH, Bm.cta0[n]);
-  k_seam_merge_batch<<<grid, 256, 0, st>>>(Bm, SwpCfg<32>::CH);
+  dim3 grid((maxw + 255) / 256, S::CH, Bm.cta0[n]);
+  k_seam_merge_batch<<<grid, 256, 0, st>>>(Bm, S::CH);
   count_launch();
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
+                                  cudaEvent_t mark) {
+  SweepBatch Bf, B, Bm;
+  if (!sweep_batches(planes, n, Bf, B, Bm)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
+  int maxw = 0;
+  for (int i = 0; i < n; i++) maxw = std::max(maxw, planes[i].inv.g.W);
+  static_assert(SwpCfg<32>::TJ == 7 && SwpCfg<16>::TJ == 15, "cells per strip");
+  return planes[0].inv.g.bw == 16 ? launch_sweep_n<16>(Bf, B, Bm, n, maxw, t, st, mark)
+                                  : launch_sweep_n<32>(Bf, B, Bm, n, maxw, t, st, mark);
 }
 
 cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
@@ -1213,15 +1259,21 @@ cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mar
 }
 
 namespace {
-template <int MINB, bool HALF>
+template <int N, int MINB, bool HALF>
 bool is_filter_h(const void* f) {
-  return f == (const void*)k_filter_tc<32, -1, MINB, HALF> || f == (const void*)k_filter_tc<32, 1, MINB, HALF> ||
-         f == (const void*)k_filter_tc<32, 2, MINB, HALF> || f == (const void*)k_filter_tc<32, 3, MINB, HALF> ||
-         f == (const void*)k_filter_tc<32, 4, MINB, HALF>;
+  return f == (const void*)k_filter_tc<N, -1, MINB, HALF> || f == (const void*)k_filter_tc<N, 1, MINB, HALF> ||
+         f == (const void*)k_filter_tc<N, 2, MINB, HALF> || f == (const void*)k_filter_tc<N, 3, MINB, HALF> ||
+         f == (const void*)k_filter_tc<N, 4, MINB, HALF>;
 }
-template <int MINB>
+template <int N>
 bool is_filter(const void* f) {
-  return is_filter_h<MINB, false>(f) || is_filter_h<MINB, true>(f);
+  return is_filter_h<N, 3, false>(f) || is_filter_h<N, 3, true>(f) || is_filter_h<N, 4, false>(f) ||
+         is_filter_h<N, 4, true>(f) || is_filter_h<N, 5, false>(f) || is_filter_h<N, 5, true>(f);
+}
+template <int N>
+bool is_forward(const void* f) {
+  return f == (const void*)k_forward_tc<N, 1, false> || f == (const void*)k_forward_tc<N, 2, false> ||
+         f == (const void*)k_forward_tc<N, 2, true> || f == (const void*)k_forward_tc<N, 4, true>;
 }
 }  // namespace
 
@@ -1236,7 +1288,7 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
   if (e != cudaSuccess) return e;
   std::vector<cudaGraphNode_t> nodes(cnt);
   if ((e = cudaGraphGetNodes(graph, nodes.data(), &cnt)) != cudaSuccess) return e;
-  int ch = SwpCfg<32>::CH;
+  int ch = (ns > 0 ? sw[0].inv.g.bh : 32) / 2;
   for (cudaGraphNode_t node : nodes) {
     cudaGraphNodeType ty;
     if ((e = cudaGraphNodeGetType(node, &ty)) != cudaSuccess) return e;
@@ -1245,12 +1297,11 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
     if ((e = cudaGraphKernelNodeGetParams(node, &kp)) != cudaSuccess) return e;
     void* args[2] = {nullptr, &ch};
     const void* f = kp.func;
-    if (f == (const void*)k_forward_tc<32, 1, false> || f == (const void*)k_forward_tc<32, 2, false> ||
-        f == (const void*)k_forward_tc<32, 2, true> || f == (const void*)k_forward_tc<32, 4, true>)
+    if (is_forward<32>(f) || is_forward<16>(f))
       args[0] = &Bw;
-    else if (is_filter<3>(f) || is_filter<4>(f) || is_filter<5>(f))
+    else if (is_filter<32>(f) || is_filter<16>(f))
       args[0] = &Bf;
-    else if (f == (const void*)k_sweep_tc<32>)
+    else if (f == (const void*)k_sweep_tc<32> || f == (const void*)k_sweep_tc<16>)
       args[0] = &Bs;
     else if (f == (const void*)k_seam_merge_batch)
       args[0] = &Bm;
@@ -1265,7 +1316,8 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
 
 size_t tc_image_bytes(const Geo& g, int strips) {
   const int cells_y = (g.H + g.bh / 2 - 1) / (g.bh / 2);
-  return (size_t)(cells_y + 1) * strips * SwpCfg<32>::TILE;
+  const size_t tile = g.bw == 16 ? SwpCfg<16>::TILE : SwpCfg<32>::TILE;
+  return (size_t)(cells_y + 1) * strips * tile;
 }
 
 }  // namespace f3d

@@ -151,7 +151,7 @@ cudaError_t launch_inverse_fast(const InvArgs& a, cudaStream_t st);
 
 // Tensor-core form (f3d_k_tc.cu): block transforms as DFT-matrix products on
 // the tensor cores, fp16 operands split into hi + lo parts, fp32
-// accumulation in tensor memory. Mode 1, square 32x32 blocks.
+// accumulation in tensor memory. Mode 1, square 16x16 or 32x32 blocks.
 struct TcFwdArgs {
   Geo g;
   const uint8_t* src;  // plane in device memory
@@ -217,7 +217,7 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
                             const SweepArgs* sw, int ns);
 // Tensor-core sweep: cells per strip, CTAs per SM, and the launches (filter,
 // inverse + overlap-add, seam merge of f3d_k_sweep.cu).
-constexpr int kTcSweepCells = 7;
+int tc_sweep_cells(int n);  // 7 for 32 x 32 blocks, 15 for 16 x 16
 constexpr int kTcSweepCtasPerSm = 3;
 cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark);
 // Bytes of SweepArgs::img for this geometry and strip count.

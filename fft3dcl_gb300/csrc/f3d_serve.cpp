@@ -120,7 +120,8 @@ void free_stream(Stream* s) {
 // conditions of its forward and sweep: mode 1, 32x32 blocks, half overlap,
 // not Kalman), so that it is created on the server's shared stream.
 bool predict_batchable(int form, const f3d_internal_params& ip) {
-  return form == F3D_FORM_TC && ip.bm != 0 && ip.mode == 1 && ip.bw == 32 && ip.bh == 32 && ip.ow * 2 == ip.bw &&
+  return form == F3D_FORM_TC && ip.bm != 0 && ip.mode == 1 && ip.bw == ip.bh && (ip.bw == 16 || ip.bw == 32) &&
+         ip.ow * 2 == ip.bw &&
          ip.oh * 2 == ip.bh;
 }
 

@@ -73,6 +73,29 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 16 consecutive 32-bit columns of this thread's tensor-memory lane, as
+// tmem_ld32.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+// M (16 or 32) consecutive columns.
+template <int M>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[M]) {
+  static_assert(M == 16 || M == 32, "tensor-memory load width");
+  if constexpr (M == 32) tmem_ld32(taddr, v);
+  else tmem_ld16(taddr, v);
+}
+
 // ---- MMA -----------------------------------------------------------------
 enum : uint32_t { LAYOUT_INTERLEAVE = 0, LAYOUT_SW128 = 2 };
 

@@ -263,7 +263,7 @@ int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
  * engine given several times) with one launch per kernel: the forward
  * transform of each plane's entering frame, then filter, inverse and
  * overlap-add of each plane's window. The engines must run the fused
- * tensor-core form (F3D_FORM_TC, half overlap, 32x32 blocks) on one device
+ * tensor-core form (F3D_FORM_TC, half overlap, 16x16 or 32x32 blocks) on one device
  * and one stream, with the same block size, overlap, window type, temporal
  * mode and sample format; plane sizes and bit depths may differ.
  * F3D_BATCH_GRAPH: each step shape is captured once as a CUDA graph and

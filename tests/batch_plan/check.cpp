@@ -122,7 +122,8 @@ int main() {
     m[1].img = nullptr;
     CHECK(!sweep_batches(m.data(), 2, Bf, Bs, Bm));
   }
-  // Forward: block-group prefix, one group per kTcGroupBlocks blocks.
+  // Forward: block-group prefix, one group per 8 blocks of 32 x 32 (16 of
+  // 16 x 16); the planes of a batch share the block size.
   {
     TcFwdArgs f[3] = {};
     const int nb[3] = {32912, 8540, 2232};
@@ -138,6 +139,12 @@ int main() {
     CHECK(B.grp0[kMaxBatch] == B.grp0[3]);
     f[2].fmt = FMT_U8;
     CHECK(!forward_batch(f, 3, B));
+    f[2].fmt = FMT_U16;
+    f[2].g.bw = f[2].g.bh = 16;
+    CHECK(!forward_batch(f, 3, B));
+    for (int i = 0; i < 3; i++) f[i].g.bw = f[i].g.bh = 16;
+    CHECK(forward_batch(f, 3, B));
+    CHECK(B.grp0[1] == 2057 && B.grp0[2] == 2057 + 534 && B.grp0[3] == 2057 + 534 + 140);
   }
   // Autotuner: the default shape (index 0) unless another is over 1 % faster.
   {

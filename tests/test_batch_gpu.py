@@ -113,6 +113,25 @@ def test_every_launch_shape_equals_engines(bt):
                 np.testing.assert_array_equal(g, r, err_msg=f"shape {shape} plane {i} frame {n}")
 
 
+@pytest.mark.parametrize("bt", [1, 3, 4])
+def test_bw16_planes_and_outputs_batch_equal_engines(bt):
+    # 16x16 blocks: YUV planes in one batch (every launch shape), and
+    # consecutive outputs of one plane, equal the engines' own calls.
+    planes = yuv420(352, 208, 6, 91 + bt, 10)
+    params = dict(sigma=3.0, bt=bt, bw=16, bh=16, sharpen=0.3)
+    ref, _ = run_planes(planes, params, [False, True, True], 10, None)
+    for shape in [(3, 5), (1, 4), (2, 3)]:
+        got, _ = run_planes(planes, params, [False, True, True], 10, 1, shape=shape)
+        for i in range(3):
+            for n, (g, r) in enumerate(zip(got[i], ref[i])):
+                np.testing.assert_array_equal(g, r, err_msg=f"shape {shape} plane {i} frame {n}")
+    frames = planes[0]
+    ref1 = F.FFT3DCL(frames, bits=10, form="tc", **params)
+    got1, _ = consecutive_outputs(frames, 10, params, 3, True)
+    for n in range(len(frames)):
+        np.testing.assert_array_equal(got1[n], ref1[n], err_msg=f"frame {n}")
+
+
 def test_batch_kernel_times():
     import torch
     frames = synth.moving_rects(320, 192, 6, 61, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)

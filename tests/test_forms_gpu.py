@@ -43,6 +43,18 @@ CASES = [
      dict(bt=1, sigma2=1.0, sigma3=3.0, sigma4=4.0)),
     ("gray8_btm1", lambda: synth.clip_gray8(frames=2), 8, dict(bt=-1, sharpen=0.7)),
     ("gray8_bw16_wintype1", lambda: synth.clip_gray8(frames=5), 8, dict(bw=16, bh=16, wintype=1)),
+    # 16x16 blocks: the tensor-core form's 16-point DFT matrices, every temporal mode.
+    ("gray8_bw16_bt4_sharpen", lambda: synth.clip_gray8(frames=6), 8, dict(bt=4, bw=16, bh=16, sharpen=0.4)),
+    ("p10_bw16_bt3", lambda: synth.moving_rects(1280, 720, 5, 21, lo=64, hi=940, noise=10.0, dtype=np.uint16,
+                                                maxval=1023), 10, dict(bt=3, bw=16, bh=16, sigma=3.0)),
+    ("p10_bw16_bt2_pattern", lambda: synth.moving_rects(400, 232, 4, 22, lo=64, hi=940, noise=10.0,
+                                                        dtype=np.uint16, maxval=1023), 10,
+     dict(bt=2, bw=16, bh=16, sigma2=1.0, sigma3=3.0, sigma4=4.0)),
+    ("gray8_bw16_bt1_wintype2", lambda: synth.clip_gray8(frames=3), 8, dict(bt=1, bw=16, bh=16, wintype=2)),
+    ("gray8_bw16_btm1", lambda: synth.clip_gray8(frames=2), 8, dict(bt=-1, bw=16, bh=16, sharpen=0.6)),
+    ("float_bw16_bt3", lambda: synth.clip_grays(frames=5), 32, dict(bt=3, bw=16, bh=16, sharpen=0.3)),
+    ("p16_bw16_bt4", lambda: synth.moving_rects(224, 128, 6, 9, lo=4096, hi=60000, noise=300.0, dtype=np.uint16,
+                                                maxval=65535), 16, dict(bt=4, bw=16, bh=16)),
     # 32x32 blocks: the tensor-core form folds these windows into its DFT matrices.
     ("gray8_wintype1", lambda: synth.clip_gray8(frames=5), 8, dict(bt=3, wintype=1, sharpen=0.3)),
     ("gray8_wintype2", lambda: synth.clip_gray8(frames=5), 8, dict(bt=4, wintype=2)),
@@ -78,7 +90,7 @@ def test_form_within_tolerance(form, name, make, bits, params):
 def test_form_spectra_close_to_oracle(form):
     rng = np.random.default_rng(1)
     plane = rng.integers(0, 256, (97, 131)).astype(np.uint8)
-    for bw, bh in [(8, 8), (16, 32), (32, 32), (64, 16), (64, 64)]:
+    for bw, bh in [(8, 8), (16, 16), (16, 32), (32, 32), (64, 16), (64, 64)]:
         with F.Engine(131, 97, 8, form=form, bw=bw, bh=bh) as e:
             e.forward_raw(0, plane)
             spec = e.spectra(0)
@@ -126,6 +138,7 @@ def test_form_golden_within_tolerance(form, path):
     check(got, out, tol_for(frames, bits))
 
 
+@pytest.mark.parametrize("bw", [16, 32])
 @pytest.mark.parametrize("w,h,params", [
     (640, 360, dict(bt=3)),
     (333, 177, dict(bt=2, sharpen=0.5)),
@@ -135,10 +148,11 @@ def test_form_golden_within_tolerance(form, path):
     (24, 20, dict(bt=3)),
     (16, 16, dict(bt=4, sharpen=0.4)),
 ])
-def test_tc_sweep_sizes(w, h, params):
+def test_tc_sweep_sizes(w, h, params, bw):
     # The tensor-core sweep on planes with ragged edges, one and many
     # segments (seam rows) and strips, against the oracle.
     frames = synth.moving_rects(w, h, 5, w + 3 * h, lo=16, hi=235, noise=4.0, n_rects=5)
+    params = dict(params, bw=bw, bh=bw)
     flt = F.Filter([[f] for f in frames], F.VideoFormat("gray", 8, 0), form="tc", **params)
     info = flt.engines[0].info()
     assert info.form == 2 and info.fused == 1

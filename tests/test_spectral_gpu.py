@@ -18,6 +18,8 @@ BOUND = {"exact": 1e-6, "fast": 1e-6, "tc": 1e-5}
 CONFIGS = [
     ("640x360_gray8_bt3", lambda: synth.clip_gray8(frames=1)[0], 8, dict(sigma=2.0, bt=3)),
     ("4k_p10_bt4", lambda: synth.clip_yuv420p10_luma(frames=1)[0], 10, dict(sigma=3.0, bt=4, sharpen=0.4)),
+    ("4k_p10_bt4_bw16", lambda: synth.clip_yuv420p10_luma(frames=1)[0], 10,
+     dict(sigma=3.0, bt=4, bw=16, bh=16, sharpen=0.4)),
 ]
 
 
