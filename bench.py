@@ -757,8 +757,8 @@ def run_gpu(args, rank, world, local_rank):
             "capacity_frames_per_s": capacity,
             "load_sweep": sweep,
             "mix": "YUV420P8/P10 video streams, all three planes (one server stream per plane), resolutions "
-                   "640x360..3840x2160, bt in {1,3,4}, bw in {16,32} (bw 16 runs the fast form on its own "
-                   "CUDA stream; the tensor-core streams share steps)",
+                   "640x360..3840x2160, bt in {1,3,4}, bw in {16,32}; every stream runs the tensor-core form and "
+                   "streams with the same block size, bt and depth share steps",
             "arrivals": "Poisson, 24-60 frames/s per stream (rate_x scales every stream's rate)",
             "latency": "per video frame: scheduled arrival of the last frame its temporal window needs -> last "
                        "plane's output copied to host memory (server_*: from that frame's arrival at the server)",

@@ -7,7 +7,9 @@
 // include/fft3d_gb300.h; there is no CPU fallback, so device=0 and any GPU
 // failure are reported as errors (mapSetError at create, setFilterError per
 // frame). The arithmetic form is taken from FFT3DCL_FORM (exact | fast | tc,
-// default exact); FFT3DCL_LOG names a file that receives one line per
+// default tc: within the reference GPU path's tolerance of its CPU backend,
+// +-1 LSB at 8 bits and +-4 at 10; exact gives the CPU backend's bits; Kalman
+// always runs exact). FFT3DCL_LOG names a file that receives one line per
 // instance created or released with the live engine count and device bytes.
 #include "VSHelper4.h"
 #include "VapourSynth4.h"
@@ -61,10 +63,10 @@ void log_usage(VSCore* core, const VSAPI* vsapi, const char* what) {
 
 int form_from_env() {
   const char* f = std::getenv("FFT3DCL_FORM");
-  if (!f) return F3D_FORM_EXACT;
+  if (!f || !*f) return F3D_FORM_TC;
+  if (!std::strcmp(f, "exact")) return F3D_FORM_EXACT;
   if (!std::strcmp(f, "fast")) return F3D_FORM_FAST;
-  if (!std::strcmp(f, "tc")) return F3D_FORM_TC;
-  return F3D_FORM_EXACT;
+  return F3D_FORM_TC;
 }
 
 inline int clamp_frame(int n, int num) { return n < 0 ? 0 : (n > num - 1 ? num - 1 : n); }

@@ -14,9 +14,10 @@ first (the window requests, src/fft3dcl.cpp:319-331), every source frame is
 freed, the filter is fmFrameState for Kalman and fmParallelRequests otherwise
 (:286-292), and no engine is left alive once the filter is freed.
 
-Tolerances: the exact form is bit-equal to the oracle; fast and tc within
-+-1 LSB at 8 bits, +-4 LSB at 10 bits, 1e-4 absolute on float samples in
-[0, 1] (Kalman runs the exact form in every form)."""
+Tolerances: the exact form is bit-equal to the oracle; fast and tc (tc is
+the plugin's default) within +-1 LSB at 8 bits, +-4 LSB at 10 bits, 1e-4
+absolute on float samples in [0, 1] (Kalman runs the exact form in every
+form)."""
 import numpy as np
 import pytest
 
@@ -35,7 +36,7 @@ def host(tmp_path_factory):
 
 
 def tol(frames, bits, form):
-    if form in (None, "exact"):
+    if form == "exact":
         return 0
     if frames[0].dtype == np.float32:
         return 1e-4
@@ -86,8 +87,9 @@ def test_gray8_plain_method_every_form(host, tmp_path):
         run_and_compare(host, tmp_path, [y], "gray", 8, {0}, form=form, sigma=2.0, beta=1.0, bt=3)
 
 
-def test_gray8_default_form_is_exact(host, tmp_path):
-    # FFT3DCL_FORM unset: the exact form, bit-equal, frames requested out of order.
+def test_gray8_default_form_is_tc(host, tmp_path):
+    # FFT3DCL_FORM unset: the tensor-core form, within +-1 LSB at 8 bits,
+    # frames requested out of order.
     y = synth.clip_gray8(width=200, height=136, frames=7)
     run_and_compare(host, tmp_path, [y], "gray", 8, {0}, form=None, order="shuffle", bt=3, sharpen=0.3)
 
