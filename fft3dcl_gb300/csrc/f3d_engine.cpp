@@ -1157,11 +1157,18 @@ bool engine_batchable(const f3d_engine* e) {
   return e && e->form == F3D_FORM_TC && e->inv_form == F3D_FORM_TC && e->fused;
 }
 
-uint64_t engine_batch_key(const f3d_engine* e) {
-  const f3d_internal_params& p = e->ip;
+namespace {
+uint64_t batch_key(const f3d_internal_params& p, int fmt, bool half) {
   return (uint64_t)p.bw | ((uint64_t)p.bh << 10) | ((uint64_t)p.ow << 20) | ((uint64_t)p.oh << 30) |
-         ((uint64_t)p.wintype << 40) | ((uint64_t)(p.bm + 1) << 42) | ((uint64_t)e->fmt << 46) |
-         ((uint64_t)e->half << 52);
+         ((uint64_t)p.wintype << 40) | ((uint64_t)(p.bm + 1) << 42) | ((uint64_t)fmt << 46) |
+         ((uint64_t)half << 52);
+}
+}  // namespace
+
+uint64_t engine_batch_key(const f3d_engine* e) { return batch_key(e->ip, e->fmt, e->half); }
+
+uint64_t plane_batch_key(const f3d_internal_params& p, const f3d_plane_geom& g) {
+  return batch_key(p, g.sample_type == 1 ? FMT_F32 : (g.bits <= 8 ? FMT_U8 : FMT_U16), false);
 }
 
 int engines_step(f3d_engine* const* eng, int n, const int* fns, const void* const* src, const size_t* src_pitch,

@@ -17,6 +17,9 @@ bool engine_batchable(const f3d_engine* e);
 // Engines with the same key may share a launch: block size, overlap, window
 // type, temporal mode, sample format and spectrum storage.
 uint64_t engine_batch_key(const f3d_engine* e);
+// The key an engine for this plane will have (without fp16 spectrum storage),
+// before it is created.
+uint64_t plane_batch_key(const f3d_internal_params& p, const f3d_plane_geom& g);
 
 // One temporal step of n (1..16) distinct batchable engines whose stream is
 // st, one launch per kernel for all of them: engine i forwards frame fns[i]

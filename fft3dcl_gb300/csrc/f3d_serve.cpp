@@ -14,12 +14,13 @@
 //    spectra (and Kalman state) stay in HBM between frames;
 //  - continuous batching: one scheduler thread launches, on every pass, the
 //    next output of every stream whose window frames have arrived. Streams
-//    that run the fused tensor-core form share one CUDA stream, and the ready
-//    outputs of all of them whose kernels take the same parameters (block
-//    size, overlap, window, temporal mode, sample format) go into one step:
-//    one launch per kernel for up to sixteen planes of any sizes. Other
-//    streams (fast or exact form, Kalman) launch on their own CUDA streams,
-//    concurrently. Streams opened while others run join the next pass;
+//    that run the fused tensor-core form are grouped by the parameters their
+//    kernels take (block size, overlap, window, temporal mode, sample
+//    format); each group has one CUDA stream, and the ready outputs of a
+//    group go into one step: one launch per kernel for up to sixteen planes
+//    of any sizes. Groups run concurrently with each other, as do the other
+//    streams (fast or exact form, Kalman) on their own CUDA streams. Streams
+//    opened while others run join the next pass;
 //  - latency: an output's latency runs from the arrival of the last input
 //    frame its window needs to the completion of its readback to host memory.
 #include "f3d_engine_internal.hpp"
@@ -85,9 +86,10 @@ struct OutSlot {
 struct Stream {
   int id = -1;
   f3d_engine* eng = nullptr;
-  cudaStream_t cs = nullptr;  // the stream's own CUDA stream, or the server's shared one (batched)
+  cudaStream_t cs = nullptr;  // the stream's own CUDA stream, or its group's (batched)
   bool own_cs = true;
   bool batched = false;       // launched in shared steps with other streams
+  uint64_t gkey = 0;          // group of a batched stream
   int W = 0, H = 0, bps = 1, nframes = 0, need = 1, cur = 0, bt = 1;
   size_t row_bytes = 0, plane_bytes = 0, est_bytes = 0;
   uint8_t* d_src = nullptr;
@@ -118,7 +120,7 @@ void free_stream(Stream* s) {
 
 // Whether a stream's engine will run the fused tensor-core form (the
 // conditions of its forward and sweep: mode 1, 32x32 blocks, half overlap,
-// not Kalman), so that it is created on the server's shared stream.
+// not Kalman), so that it is created on its group's CUDA stream.
 bool predict_batchable(int form, const f3d_internal_params& ip) {
   return form == F3D_FORM_TC && ip.bm != 0 && ip.mode == 1 && ip.bw == ip.bh && (ip.bw == 16 || ip.bw == 32) &&
          ip.ow * 2 == ip.bw &&
@@ -129,8 +131,14 @@ bool predict_batchable(int form, const f3d_internal_params& ip) {
 
 struct f3d_server {
   f3d_server_config cfg{};
-  cudaStream_t shared = nullptr;  // CUDA stream of the batched streams
-  std::deque<cudaEvent_t> inflight, spare;  // end events of the queued shared steps, unused ones
+  // Groups of batched streams: one CUDA stream each, and the end events of
+  // the shared steps queued on it.
+  struct Group {
+    cudaStream_t cs = nullptr;
+    std::deque<cudaEvent_t> inflight;
+  };
+  std::map<uint64_t, Group> groups;
+  std::deque<cudaEvent_t> spare;  // unused step events
   long long steps = 0, step_outputs = 0;
   int max_step = 0;
   std::mutex mtx;
@@ -147,7 +155,7 @@ struct f3d_server {
   bool ready(Stream* s, int n, std::vector<int>& win);
   void launch(Stream* s, int n, const std::vector<int>& win);
   bool launch_shared();
-  void step_group(std::vector<Stream*>& grp);
+  void step_group(std::vector<Stream*>& grp, cudaStream_t cs);
   void reap(Stream* s);
 };
 
@@ -219,29 +227,28 @@ void f3d_server::reap(Stream* s) {
 // and whose kernels take the same parameters (at most sixteen streams a
 // step). Returns whether anything was launched.
 bool f3d_server::launch_shared() {
-  while (!inflight.empty() && cudaEventQuery(inflight.front()) == cudaSuccess) {
-    spare.push_back(inflight.front());
-    inflight.pop_front();
-  }
-  if ((int)inflight.size() >= kMaxInflight) return false;
-  std::map<uint64_t, std::vector<Stream*>> groups;
+  std::map<uint64_t, std::vector<Stream*>> ready_by_group;
   std::vector<int> win;
   for (auto& kv : streams) {
     Stream* s = kv.second;
     if (!s->batched || !s->err.empty() || s->next_out >= s->nframes || (int)s->outs.size() >= kOutSlots) continue;
     if (!ready(s, s->next_out, win)) continue;
-    groups[f3d::engine_batch_key(s->eng)].push_back(s);
+    ready_by_group[s->gkey].push_back(s);
   }
   bool any = false;
-  for (auto& kv : groups) {
+  for (auto& kv : ready_by_group) {
+    Group& g = groups[kv.first];
+    while (!g.inflight.empty() && cudaEventQuery(g.inflight.front()) == cudaSuccess) {
+      spare.push_back(g.inflight.front());
+      g.inflight.pop_front();
+    }
+    if ((int)g.inflight.size() >= kMaxInflight) continue;
     std::vector<Stream*>& all = kv.second;
     for (size_t i = 0; i < all.size(); i += 16) {
       std::vector<Stream*> grp(all.begin() + i, all.begin() + std::min(all.size(), i + 16));
-      step_group(grp);
-      any = true;
+      step_group(grp, g.cs);
     }
-  }
-  if (any) {
+    any = true;
     cudaEvent_t ev = nullptr;
     if (!spare.empty()) {
       ev = spare.back();
@@ -251,8 +258,8 @@ bool f3d_server::launch_shared() {
       ev = nullptr;
     }
     if (ev) {
-      cudaEventRecord(ev, shared);
-      inflight.push_back(ev);
+      cudaEventRecord(ev, g.cs);
+      g.inflight.push_back(ev);
     }
   }
   return any;
@@ -261,7 +268,7 @@ bool f3d_server::launch_shared() {
 // The next output of every stream of grp in shared steps: the window frames
 // not cached yet go up one per stream and step (forward only), the last
 // with the outputs; then each output is copied to its host slot.
-void f3d_server::step_group(std::vector<Stream*>& grp) {
+void f3d_server::step_group(std::vector<Stream*>& grp, cudaStream_t shared) {
   const int n = (int)grp.size();
   std::vector<std::vector<int>> wins(n), missing(n);
   std::vector<double> t_ready(n, 0.0);
@@ -385,11 +392,6 @@ int f3d_server_create(const f3d_server_config* cfg, f3d_server** out) {
   auto* sv = new f3d_server();
   sv->cfg = *cfg;
   cudaSetDevice(cfg->device);
-  if (cudaStreamCreateWithFlags(&sv->shared, cudaStreamNonBlocking) != cudaSuccess) {
-    cudaGetLastError();
-    delete sv;
-    return fail(F3D_E_CUDA, "FFT3DCL: server stream creation failed");
-  }
   sv->worker = std::thread([sv] { sv->run(); });
   *out = sv;
   return F3D_OK;
@@ -402,9 +404,11 @@ void f3d_server_destroy(f3d_server* sv) {
   if (sv->worker.joinable()) sv->worker.join();
   cudaSetDevice(sv->cfg.device);
   for (auto& kv : sv->streams) free_stream(kv.second);
-  for (cudaEvent_t ev : sv->inflight) cudaEventDestroy(ev);
+  for (auto& kv : sv->groups) {
+    for (cudaEvent_t ev : kv.second.inflight) cudaEventDestroy(ev);
+    if (kv.second.cs) cudaStreamDestroy(kv.second.cs);
+  }
   for (cudaEvent_t ev : sv->spare) cudaEventDestroy(ev);
-  if (sv->shared) cudaStreamDestroy(sv->shared);
   delete sv;
 }
 
@@ -421,7 +425,15 @@ int f3d_server_open(f3d_server* sv, const f3d_script_params* sp, const f3d_plane
   if (rc != F3D_OK) return rc;
   auto s = std::unique_ptr<Stream, void (*)(Stream*)>(new Stream(), free_stream);
   if (predict_batchable(sv->cfg.form, ip)) {
-    s->cs = sv->shared;
+    s->gkey = f3d::plane_batch_key(ip, *geom);
+    std::lock_guard<std::mutex> lk(sv->mtx);
+    f3d_server::Group& g = sv->groups[s->gkey];
+    if (!g.cs && cudaStreamCreateWithFlags(&g.cs, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      g.cs = nullptr;
+      return fail(F3D_E_CUDA, "FFT3DCL: stream creation failed");
+    }
+    s->cs = g.cs;
     s->own_cs = false;
   } else if (cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking) != cudaSuccess) {
     return fail(F3D_E_CUDA, "FFT3DCL: stream creation failed");

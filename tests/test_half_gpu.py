@@ -28,7 +28,8 @@ def worst_diff(got, ref):
     (8, "tc", dict(precision=2), False),
     (10, "tc", dict(precision=0), False),     # forced to precision 2 above 8 bits
     (8, "fast", dict(precision=0), False),
-    (8, "tc", dict(precision=0, bw=16, bh=16), False),  # tensor-core forward, fast-form inverse
+    (8, "tc", dict(precision=0, bw=16, bh=16), True),
+    (8, "tc", dict(precision=0, ow=8, oh=8), False),  # tensor-core forward, fast-form inverse
 ])
 def test_half_storage_applies_where_the_original_used_it(bits, form, params, applies):
     with F.Engine(320, 192, bits, form=form, flags=HALF, **params) as e:
@@ -45,6 +46,7 @@ CASES = [
     ("gray8_bt1_pattern", lambda: synth.clip_gray8(frames=3), dict(bt=1, sigma2=1.0, sigma3=3.0, sigma4=4.0,
                                                                    precision=0)),
     ("gray8_btm1", lambda: synth.clip_gray8(frames=2), dict(bt=-1, sharpen=0.7, precision=0)),
+    ("gray8_bw16_bt4", lambda: synth.clip_gray8(frames=6), dict(bt=4, bw=16, bh=16, sharpen=0.3, precision=0)),
 ]
 
 
