@@ -48,9 +48,10 @@ NCU_TRAFFIC = {"tc": 571806464 + 130638592}
 # (k -> bytes): captured on the 1920x1080 case of this workload (`--size
 # 1920x1080 --steps 1 --warmup 3 --no-cpu --serve-streams 0 --no-yuv
 # --compare tc --outputs-per-step k`, mean of the k-output launches; k=4:
-# 260.2 MB read + 124.4 MB written, k=8: 410.5 + 286.0 MB, k=10: 487.5 +
-# 365.7 MB) and scaled to 3840x2160 by the block count (32912 / 8540).
-NCU_TRAFFIC_BATCH = {4: 1002927925 + 479516689, 8: 1581975962 + 1102231724, 10: 1878657040 + 1409240147}
+# 260.2 MB read + 124.4 MB written, k=8: 410.5 + 286.0 MB, k=10 (with the
+# filter's current column mapping): 490.3 + 366.7 MB) and scaled to
+# 3840x2160 by the block count (32912 / 8540).
+NCU_TRAFFIC_BATCH = {4: 1002927925 + 479516689, 8: 1581975962 + 1102231724, 10: 1889588860 + 1413116250}
 # Consecutive outputs per batch step of the tensor-core headline (4K sweeps:
 # ten beat eight and twelve); its traffic must be in NCU_TRAFFIC_BATCH.
 DEFAULT_OUTPUTS_PER_STEP = 10

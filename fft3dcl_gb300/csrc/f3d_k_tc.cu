@@ -140,6 +140,10 @@ struct Gather {
 template <int N, int BPS>
 __device__ __forceinline__ void fetch(const TcFwdArgs& a, int b0, int nvalid, uint4 (&r)[Gather<N, BPS>::TPT]) {
   using Gt = Gather<N, BPS>;
+  // The group's blocks are consecutive in the mode-1 grid (the only mode of
+  // this form): one division for the first, a carry into the next block row
+  // for the others.
+  const int m0 = b0 / a.g.ncols, n0 = b0 - m0 * a.g.ncols;
 #pragma unroll
   for (int i = 0; i < Gt::TPT; i++) {
     const int q = threadIdx.x + i * kTcThreads;
@@ -147,8 +151,12 @@ __device__ __forceinline__ void fetch(const TcFwdArgs& a, int b0, int nvalid, ui
     const int bl = ry / N, y = ry - bl * N;
     r[i] = make_uint4(0u, 0u, 0u, 0u);
     if (bl >= nvalid) continue;
-    int bx, by, par;
-    block_origin(a.g, b0 + bl, bx, by, par);
+    int n = n0 + bl, m = m0;
+    while (n >= a.g.ncols) {
+      n -= a.g.ncols;
+      m++;
+    }
+    const int bx = a.g.xoff + n * a.g.xstep, by = a.g.yoff + m * a.g.ystep;
     if (bx >= 0 && by >= 0 && bx + N <= a.g.W && by + N <= a.g.H) {
       const uint8_t* p = a.src + (long long)(by + y) * a.pitch + (long long)bx * BPS + 16 * c;
       if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
@@ -179,6 +187,18 @@ __device__ __forceinline__ void deposit(const TcFwdArgs& a, uint8_t* a1, const u
   using Gt = Gather<N, BPS>;
   using C = TcCfg<N>;
   const bool split = SPLIT && a.split;
+  // Integer samples below 1024 become fp16 exactly by exponent bias: 0x6400
+  // is 1024.0, and its ten mantissa bits hold the sample, so (0x6400 | v) -
+  // 1024 = v, two instructions per pair. Samples of 1024 and above (11-bit
+  // clips) take the conversion through fp32.
+  bool small = BPS == 1;
+  if (BPS == 2 && !split) {
+    uint32_t hi_bits = 0u;
+#pragma unroll
+    for (int i = 0; i < Gt::TPT; i++) hi_bits |= r[i].x | r[i].y | r[i].z | r[i].w;
+    small = (hi_bits & 0xFC00FC00u) == 0u;
+  }
+  const __half2 k1024 = __halves2half2(__ushort_as_half(0x6400), __ushort_as_half(0x6400));
 #pragma unroll
   for (int i = 0; i < Gt::TPT; i++) {
     const int q = threadIdx.x + i * kTcThreads;
@@ -186,16 +206,28 @@ __device__ __forceinline__ void deposit(const TcFwdArgs& a, uint8_t* a1, const u
     const int bl = ry / N, y = ry - bl * N;
     const int tile = bl / C::BPT1, row = (bl % C::BPT1) * N + y;
     const uint32_t w[4] = {r[i].x, r[i].y, r[i].z, r[i].w};
-    float v[Gt::S];
-#pragma unroll
-    for (int k = 0; k < Gt::S; k++) {
-      if (BPS == 1) v[k] = (float)((w[k >> 2] >> (8 * (k & 3))) & 0xffu);
-      else if (BPS == 2) v[k] = (float)((w[k >> 1] >> (16 * (k & 1))) & 0xffffu) * (split ? a.norm : 1.0f);
-      else v[k] = __uint_as_float(w[k]);
-    }
     uint32_t h[Gt::S / 2], l[Gt::S / 2];
+    if (BPS <= 2 && small) {
 #pragma unroll
-    for (int k = 0; k < Gt::S / 2; k++) tc::split_pair(v[2 * k], v[2 * k + 1], h[k], l[k]);
+      for (int k = 0; k < Gt::S / 2; k++) {
+        // The pair (sample 2k, sample 2k+1) with 0x64 as each one's high byte.
+        const uint32_t biased = BPS == 1 ? __byte_perm(w[k >> 1], 0x64646464u, (k & 1) ? 0x4342u : 0x4140u)
+                                         : (w[k] | 0x64006400u);
+        const __half2 hv = __hsub2(*reinterpret_cast<const __half2*>(&biased), k1024);
+        h[k] = *reinterpret_cast<const uint32_t*>(&hv);
+        l[k] = 0u;
+      }
+    } else {
+      float v[Gt::S];
+#pragma unroll
+      for (int k = 0; k < Gt::S; k++) {
+        if (BPS == 1) v[k] = (float)((w[k >> 2] >> (8 * (k & 3))) & 0xffu);
+        else if (BPS == 2) v[k] = (float)((w[k >> 1] >> (16 * (k & 1))) & 0xffffu) * (split ? a.norm : 1.0f);
+        else v[k] = __uint_as_float(w[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < Gt::S / 2; k++) tc::split_pair(v[2 * k], v[2 * k + 1], h[k], l[k]);
+    }
     uint8_t* t0 = a1 + tile * FwdSmem<N, SPLIT>::A1_TILE;
     const int x0 = c * Gt::S;
     if (Gt::S >= 8) {
