@@ -731,6 +731,13 @@ def run_gpu(args, rank, world, local_rank):
                           hbm_budget=200 << 30) as sv:
                 return serving.run(sv, specs, sframes, realtime=True, rate=rate, timeout_s=300, keep_outputs=False)[1]
 
+        # Warm-up, untimed: the same mix with a few frames per stream, all at
+        # once, so that every kernel of the mix is loaded before the timed runs.
+        wspecs = serving.mixed_streams(args.serve_streams, 8)
+        with F.Server(form=args.form, device=local_rank, max_streams=3 * len(wspecs), hbm_budget=200 << 30) as sv:
+            serving.run(sv, wspecs, [serving.stream_frames(s, distinct=4) for s in wspecs], realtime=False,
+                        timeout_s=300, keep_outputs=False)
+
         def point(rate, st):
             return {"rate_x": rate, "offered_frames_per_s": round(st["offered_frames_per_s"], 1),
                     "frames_per_s": round(st["frames_per_s"], 1), "p50_ms": round(st["p50_ms"], 3),
