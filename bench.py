@@ -146,7 +146,7 @@ def make_clip(nframes: int = NFRAMES):
 # --------------------------------------------------------------- CPU leg --
 
 def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_steps: int = 1,
-                     bits: int = BITS, params: dict | None = None):
+                     bits: int = BITS, params: dict | None = None, chroma: bool = False):
     """Oracle (the C restatement of the reference CPU backend) in steady
     state: per step one new frame is uploaded and transformed, then the
     window is filtered, inverted, overlap-added and downloaded (Kalman:
@@ -157,7 +157,7 @@ def cpu_steady_state(frames, threads: int, budget_s: float, max_steps: int, min_
     L = oracle.lib()
     h, w = frames[0].shape
     st = 1 if frames[0].dtype == np.float32 else 0
-    pl = oracle.Plane(w, h, bits, st, **params)
+    pl = oracle.Plane(w, h, bits, st, chroma=chroma, **params)
     pl.build_degrid()
     n = pl.nb * pl.fbw * pl.ip.bh
     bm = pl.ip.bm
@@ -204,6 +204,9 @@ KALMAN_PARAMS = dict(bt=0, kratio=2.0, bw=64, bh=64, ow=32, oh=32, sigma=2.0, si
 # + 2 x 16 B of state x 2,128,896 bins.
 AB_GRAY8 = 2 * 640 * 360 + 1008 * 17 * 32 * 8 * 4
 AB_KALMAN = 2 * 1280 * 720 * 4 + 2 * 16 * 1008 * 33 * 64
+# 1920x1080 YUV420P8 bt=4, all planes: luma 2 x 2,073,600 + 37,167,360 x
+# (1 + 4), each chroma plane 2 x 518,400 + 9,713,664 x (1 + 4).
+AB_YUV1080 = 2 * 1920 * 1080 + 8540 * 17 * 32 * 8 * 5 + 2 * (2 * 960 * 540 + 2232 * 17 * 32 * 8 * 5)
 
 
 def config_section(args, dev, local_rank, frames, bits, params, forms, ab_bytes, peak, kbatch=1):
@@ -286,7 +289,7 @@ YUV_PARAMS = dict(sigma=2.5, bt=4, bw=32, bh=32, ow=16, oh=16, sharpen=0.4, scut
                   smax=20.0, degrid=1.0)
 
 
-def yuv_batched(args, dev, local_rank):
+def yuv_batched(args, dev, local_rank, peak):
     """1920x1080 YUV420P8, all three planes: the tensor-core form as one
     batch (one launch per kernel for the three planes, or for four consecutive
     frames' twelve planes, replayed as a CUDA graph, autotuned) against the fast
@@ -353,8 +356,11 @@ def yuv_batched(args, dev, local_rank):
         e1.record(st)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1)
-        res[name] = {"frames_per_s": round(nsteps * k / (ms / 1000.0), 1),
-                     "launches_per_frame": round((F.kernel_launches() - l0) / (nsteps * k), 2)}
+        fps = nsteps * k / (ms / 1000.0)
+        res[name] = {"frames_per_s": round(fps, 1),
+                     "launches_per_frame": round((F.kernel_launches() - l0) / (nsteps * k), 2),
+                     "roofline_step": {"algorithmic_bytes": AB_YUV1080, "achieved": round(AB_YUV1080 * fps / 1e9, 1),
+                                       "unit": "GB/s", "frac": round(AB_YUV1080 * fps / 1e9 / peak, 4)}}
         if batch is not None:
             res[name]["tune"] = batch.tune()
             batch.close()
@@ -368,6 +374,19 @@ def yuv_batched(args, dev, local_rank):
                               "storage at precision 0, the default; opt-in, within +-1 LSB of the fp32 path)")
     res["tc_half_4frames"]["form"] = "as tc_4frames with fp16 spectrum storage"
     res["fast"]["form"] = "fp32 radix FFT, per-plane engines"
+    if not args.no_cpu:
+        # The oracle on every host thread, plane after plane: a frame takes
+        # the sum of its three planes' times.
+        threads = os.cpu_count() or 1
+        secs, steps = 0.0, []
+        for i, p in enumerate(planes):
+            fps_p, n_p = cpu_steady_state(p, threads, 2.0, 100, bits=8, params=YUV_PARAMS, chroma=i > 0)
+            secs += 1.0 / fps_p
+            steps.append(n_p)
+        res["cpu_baseline"] = {"value": round(1.0 / secs, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"steady-state output frames per plane (Y, U, V: {steps}, about 2 s "
+                                         f"each) on {threads} host threads, C restatement of src/cpu, "
+                                         "bit-identical to the reference"}
     return res
 
 
@@ -702,7 +721,7 @@ def run_gpu(args, rank, world, local_rank):
     if world == 1 and not args.no_yuv:
         line["yuv1080p_all_planes"] = dict(
             workload="1920x1080 YUV420P8 all planes, sigma=2.5 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4 scutoff=0.3 "
-                     "svr=1 smin=4 smax=20 degrid=1, clip resident in HBM", **yuv_batched(args, dev, local_rank))
+                     "svr=1 smin=4 smax=20 degrid=1, clip resident in HBM", **yuv_batched(args, dev, local_rank, peak))
     if world == 1 and not args.no_configs:
         from fft3dcl_gb300 import synth
         line["gray8_640x360_bt3"] = dict(

@@ -148,6 +148,21 @@ __device__ __forceinline__ BinTables bin_tables(const InvArgs& a, int i) {
   return t;
 }
 
+// Kalman state of one bin as read before its update (a.kalman_init: unused).
+struct KState {
+  float2 last;
+  float cov, proc;
+};
+__device__ __forceinline__ KState load_kstate(const InvArgs& a, size_t gi) {
+  KState k{make_float2(0.0f, 0.0f), 0.0f, 0.0f};
+  if (!a.kalman_init) {
+    k.last = a.klast[gi];
+    k.cov = a.kcov[gi];
+    k.proc = a.kproc[gi];
+  }
+  return k;
+}
+
 // Temporal filter + sharpen of bin i (0 <= i < bh*fbw) of a block whose
 // current-frame DC is dc, with tb the bin's tables (bin_tables(a, i)),
 // gi = b*bh*fbw + i and sv the bin's window spectra (load_window). Follows
@@ -156,9 +171,11 @@ __device__ __forceinline__ BinTables bin_tables(const InvArgs& a, int i) {
 // bm -1 pass-through, then sharpen. FAST evaluates the 3- and 4-point
 // temporal transforms with fewer additions (a different rounding; the exact
 // form keeps the reference's expressions).
+// ks: the bin's Kalman state (bm 0) as load_kstate read it, so that a
+// caller can issue the loads of several bins before their updates.
 template <int BM, bool FAST = false>
-__device__ __forceinline__ float2 filter_vals_t(const InvArgs& a, float dc, const BinTables& tb, size_t gi,
-                                                const float2 (&sv)[4]) {
+__device__ __forceinline__ float2 filter_vals_ks(const InvArgs& a, float dc, const BinTables& tb, size_t gi,
+                                                 const float2 (&sv)[4], const KState& ks) {
   float d_re = 0.0f, d_im = 0.0f;
   if (a.dg) {
     const float2 g = tb.gs;
@@ -304,8 +321,8 @@ __device__ __forceinline__ float2 filter_vals_t(const InvArgs& a, float dc, cons
       l = c;
       s = cn + cn;
     } else {
-      l = a.klast[gi];
-      s = a.kcov[gi] + a.kproc[gi];
+      l = ks.last;
+      s = ks.cov + ks.proc;
     }
     float dr = c.x - l.x, di = c.y - l.y;
     float a2 = dr * dr, b2 = di * di;
@@ -350,6 +367,16 @@ __device__ __forceinline__ float2 filter_vals_t(const InvArgs& a, float dc, cons
     fi = im;
   }
   return make_float2(fr, fi);
+}
+
+// filter_vals_ks with the Kalman state read here.
+template <int BM, bool FAST = false>
+__device__ __forceinline__ float2 filter_vals_t(const InvArgs& a, float dc, const BinTables& tb, size_t gi,
+                                                const float2 (&sv)[4]) {
+  const int bm = BM == kRuntimeBm ? a.bm : BM;
+  KState ks{make_float2(0.0f, 0.0f), 0.0f, 0.0f};
+  if (bm == 0) ks = load_kstate(a, gi);
+  return filter_vals_ks<BM, FAST>(a, dc, tb, gi, sv, ks);
 }
 
 template <int BM, bool FAST = false>

@@ -29,6 +29,12 @@ struct Cfg {
   static constexpr int TS = BW + 1;                   // padded row stride
   static constexpr int FWD_FLOATS = BH * TS + 2 * PS; // input tile + row spectra
   static constexpr int INV_FLOATS = 2 * PS + 2 * BH * TS;
+  // Loads in flight per thread: the gather takes GB samples (and window
+  // values) per round, the Kalman filter KB bins (spectrum, state, tables)
+  // before any of their results is stored.
+  static constexpr int GB = BW * BH / TPB < 16 ? BW * BH / TPB : 16;
+  static constexpr int NJ = (PS + TPB - 1) / TPB;
+  static constexpr int KB = NJ < 8 ? NJ : 8;
 };
 
 // One block: gather with mirror addressing, convert, subtract chroma
@@ -50,13 +56,26 @@ __global__ void __launch_bounds__(Cfg<BW, BH>::THREADS)
     int bx, by, par;
     block_origin(a.g, b, bx, by, par);
     const bool inside = bx >= 0 && by >= 0 && bx + BW <= a.g.W && by + BH <= a.g.H;
-    for (int idx = t; idx < BW * BH; idx += C::TPB) {
-      const int ly = idx / BW, lx = idx - ly * BW;
-      const int y = inside ? by + ly : mirror_i(by + ly, a.g.H);
-      const int x = inside ? bx + lx : mirror_i(bx + lx, a.g.W);
-      float v = load_sample(a.src + (long long)y * a.pitch, x, a.fmt, a.norm);
-      v -= a.chroma_norm;
-      tile[ly * C::TS + lx] = v * a.win[idx];
+    for (int i0 = 0; i0 < BW * BH; i0 += C::GB * C::TPB) {
+      float v[C::GB], w[C::GB];
+#pragma unroll
+      for (int u = 0; u < C::GB; u++) {
+        const int idx = i0 + t + u * C::TPB;
+        if (idx >= BW * BH) continue;
+        const int ly = idx / BW, lx = idx - ly * BW;
+        const int y = inside ? by + ly : mirror_i(by + ly, a.g.H);
+        const int x = inside ? bx + lx : mirror_i(bx + lx, a.g.W);
+        v[u] = load_sample(a.src + (long long)y * a.pitch, x, a.fmt, a.norm);
+        w[u] = a.win[idx];
+      }
+#pragma unroll
+      for (int u = 0; u < C::GB; u++) {
+        const int idx = i0 + t + u * C::TPB;
+        if (idx >= BW * BH) continue;
+        const int ly = idx / BW, lx = idx - ly * BW;
+        const float c = v[u] - a.chroma_norm;
+        tile[ly * C::TS + lx] = c * w[u];
+      }
     }
   }
   __syncthreads();
@@ -86,8 +105,11 @@ __global__ void __launch_bounds__(Cfg<BW, BH>::THREADS)
 
 // One block: temporal filter + sharpen per bin, Hermitian completion and
 // column inverse FFTs, row inverse FFTs, real part times the synthesis
-// window (src/cpu/reference.cpp:246-430, src/cpu/fft.cpp:88-119).
-template <int BW, int BH>
+// window (src/cpu/reference.cpp:246-430, src/cpu/fft.cpp:88-119). KALMAN:
+// the Kalman filter (bm 0), whose state loads of KB bins are issued before
+// their updates are stored (the compiler cannot move a bin's loads above the
+// previous bin's state stores); the other modes read bm at run time.
+template <int BW, int BH, bool KALMAN>
 __global__ void __launch_bounds__(Cfg<BW, BH>::THREADS)
     k_inverse_exact(const __grid_constant__ InvArgs a) {
   using C = Cfg<BW, BH>;
@@ -99,7 +121,29 @@ __global__ void __launch_bounds__(Cfg<BW, BH>::THREADS)
   float2* F = reinterpret_cast<float2*>(smem + slot * C::INV_FLOATS);
   float2* G = F + C::PS;
 
-  if (valid) {
+  if (valid && KALMAN) {
+    const size_t base = (size_t)b * C::PS;
+    const float dc = block_dc(a, b);
+    for (int j0 = 0; j0 < C::NJ; j0 += C::KB) {
+      float2 sv[C::KB][4];
+      KState ks[C::KB];
+      BinTables tb[C::KB];
+#pragma unroll
+      for (int u = 0; u < C::KB; u++) {
+        const int i = t + (j0 + u) * C::TPB;
+        if (j0 + u >= C::NJ || i >= C::PS) continue;
+        load_window<0>(a, base + i, sv[u]);
+        ks[u] = load_kstate(a, base + i);
+        tb[u] = bin_tables(a, i);
+      }
+#pragma unroll
+      for (int u = 0; u < C::KB; u++) {
+        const int i = t + (j0 + u) * C::TPB;
+        if (j0 + u >= C::NJ || i >= C::PS) continue;
+        F[i] = filter_vals_ks<0>(a, dc, tb[u], base + i, sv[u], ks[u]);
+      }
+    }
+  } else if (valid) {
     const size_t base = (size_t)b * C::PS;
     for (int i = t; i < C::PS; i += C::TPB) F[i] = filter_bin(a, b, i, base + i);
   }
@@ -158,7 +202,7 @@ template <int BW, int BH>
 cudaError_t launch_inv(const InvArgs& a, cudaStream_t st) {
   using C = Cfg<BW, BH>;
   const size_t smem = sizeof(float) * C::INV_FLOATS * C::BPC;
-  auto k = k_inverse_exact<BW, BH>;
+  auto k = a.bm == 0 ? k_inverse_exact<BW, BH, true> : k_inverse_exact<BW, BH, false>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

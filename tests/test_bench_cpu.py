@@ -40,3 +40,7 @@ def test_algorithmic_bytes_of_the_other_workloads():
     k = oracle.Plane(1280, 720, 32, 1, **bench.KALMAN_PARAMS)
     bins = k.nb * k.fbw * k.ip.bh
     assert bench.AB_KALMAN == 2 * 1280 * 720 * 4 + 2 * 16 * bins == 75497472
+    y = oracle.Plane(1920, 1080, 8, **bench.YUV_PARAMS)
+    u = oracle.Plane(960, 540, 8, chroma=True, **bench.YUV_PARAMS)
+    sy, su = (p.nb * p.fbw * p.ip.bh * 8 for p in (y, u))
+    assert bench.AB_YUV1080 == 2 * 1920 * 1080 + sy * 5 + 2 * (2 * 960 * 540 + su * 5) == 289187840
