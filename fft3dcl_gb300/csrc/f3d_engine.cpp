@@ -993,8 +993,9 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   if (nf == 0 && ns == 0) return F3D_OK;
   // When no plane's entering frame is in its own window (the caller runs one
   // frame ahead), the forward does not feed this step's outputs: it runs on a
-  // side stream, concurrently with filter and inverse, and joins the main
-  // stream at the end of the step (the next step's outputs need it).
+  // side stream once the filter is done, concurrently with the inverse, and
+  // joins the main stream at the end of the step (the next step's outputs
+  // need it).
   bool overlap = nf > 0 && ns > 0;
   for (int i = 0; i < n && overlap; i++)
     if (fns[i] >= 0 && (mask & (1ull << i)))
@@ -1004,12 +1005,12 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
             if (windows[j][k] == fns[i]) overlap = false;
   if (overlap) mask |= 1ull << 32;
   // Filter, inverse and seam merge; timed by events unless being captured.
-  auto sweep = [&](const TcTune& t) -> cudaError_t {
+  auto sweep = [&](const TcTune& t, cudaEvent_t after_filter) -> cudaError_t {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(b->stream, &cs);
     const bool timed = cs == cudaStreamCaptureStatusNone;
     if (timed) cudaEventRecord(b->kev[0], b->stream);
-    cudaError_t ce = launch_sweep_tc_batch(sa, ns, t, b->stream, timed ? b->kev[1] : nullptr);
+    cudaError_t ce = launch_sweep_tc_batch(sa, ns, t, b->stream, timed ? b->kev[1] : nullptr, after_filter);
     if (timed && ce == cudaSuccess) {
       cudaEventRecord(b->kev[2], b->stream);
       b->ktimed = true;
@@ -1019,16 +1020,15 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   auto launch = [&](const TcTune& t) -> cudaError_t {
     cudaError_t ce = cudaSuccess;
     if (overlap) {
-      ce = cudaEventRecord(b->fork, b->stream);
+      ce = sweep(t, b->fork);
       if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
       if (ce == cudaSuccess) ce = launch_forward_tc_batch(fa, nf, t, b->side);
       if (ce == cudaSuccess) ce = cudaEventRecord(b->join, b->side);
-      if (ce == cudaSuccess) ce = sweep(t);
       if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->stream, b->join, 0);
       return ce;
     }
     ce = nf ? launch_forward_tc_batch(fa, nf, t, b->stream) : cudaSuccess;
-    if (ce == cudaSuccess && ns) ce = sweep(t);
+    if (ce == cudaSuccess && ns) ce = sweep(t, nullptr);
     return ce;
   };
   // Autotuner: on the first step in which every plane enters a new frame,

@@ -1247,7 +1247,7 @@ namespace {
 
 template <int N>
 cudaError_t launch_sweep_n(const SweepBatch& Bf, const SweepBatch& B, const SweepBatch& Bm, int n, int maxw,
-                           const TcTune& t, cudaStream_t st, cudaEvent_t mark) {
+                           const TcTune& t, cudaStream_t st, cudaEvent_t mark, cudaEvent_t after_filter) {
   using S = SwpCfg<N>;
   const int bm = B.p[0].inv.bm;
   constexpr size_t smem = S::BYTES;
@@ -1258,6 +1258,7 @@ cudaError_t launch_sweep_n(const SweepBatch& Bf, const SweepBatch& B, const Swee
                                        : launch_filter<N, 5>(Bf, bm, st);
   if (e != cudaSuccess) return e;
   if (mark) cudaEventRecord(mark, st);
+  if (after_filter && (e = cudaEventRecord(after_filter, st)) != cudaSuccess) return e;
   // Inverse + overlap-add: one CTA per (strip, segment) of every plane.
   e = prepare(k_sweep_tc<N>, smem);
   if (e != cudaSuccess) return e;
@@ -1276,14 +1277,14 @@ cudaError_t launch_sweep_n(const SweepBatch& Bf, const SweepBatch& B, const Swee
 }  // namespace
 
 cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
-                                  cudaEvent_t mark) {
+                                  cudaEvent_t mark, cudaEvent_t after_filter) {
   SweepBatch Bf, B, Bm;
   if (!sweep_batches(planes, n, Bf, B, Bm)) return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
   int maxw = 0;
   for (int i = 0; i < n; i++) maxw = std::max(maxw, planes[i].inv.g.W);
   static_assert(SwpCfg<32>::TJ == 7 && SwpCfg<16>::TJ == 15, "cells per strip");
-  return planes[0].inv.g.bw == 16 ? launch_sweep_n<16>(Bf, B, Bm, n, maxw, t, st, mark)
-                                  : launch_sweep_n<32>(Bf, B, Bm, n, maxw, t, st, mark);
+  return planes[0].inv.g.bw == 16 ? launch_sweep_n<16>(Bf, B, Bm, n, maxw, t, st, mark, after_filter)
+                                  : launch_sweep_n<32>(Bf, B, Bm, n, maxw, t, st, mark, after_filter);
 }
 
 cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {

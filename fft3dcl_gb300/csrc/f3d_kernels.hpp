@@ -208,8 +208,10 @@ struct TcTune {
   int filter_minb = 5;      // filter kernel variant: 5, 4 or 3 CTAs per SM (spectra loads of 1, 2, 2 blocks in flight)
 };
 cudaError_t launch_forward_tc_batch(const TcFwdArgs* planes, int n, const TcTune& t, cudaStream_t st);
+// mark and after_filter (either may be null) are recorded on st between the
+// filter and the inverse kernels.
 cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
-                                  cudaEvent_t mark);
+                                  cudaEvent_t mark, cudaEvent_t after_filter = nullptr);
 // Re-points the kernel nodes of a graph captured from launch_forward_tc_batch
 // (nf planes, 0: none) + launch_sweep_tc_batch (ns planes) at new plane
 // arguments of the same shapes.
