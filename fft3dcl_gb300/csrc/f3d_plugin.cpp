@@ -11,10 +11,15 @@
 // +-1 LSB at 8 bits and +-4 at 10; exact gives the CPU backend's bits; Kalman
 // always runs exact). FFT3DCL_LOG names a file that receives one line per
 // instance created or released with the live engine count and device bytes.
+// FFT3DCL_TIME names a file to which every released instance appends the
+// process-wide time per stage of the frame path (src/timing.h:1-31 of the
+// reference): wall-clock spans of getFrame, and the device time of the
+// engine's kernels from its CUDA events.
 #include "VSHelper4.h"
 #include "VapourSynth4.h"
 #include "fft3d_gb300.h"
 
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -25,6 +30,72 @@
 #include <vector>
 
 namespace {
+
+// ---- stage timing (FFT3DCL_TIME) ----
+
+enum Stage {
+  kFetch,      // getFrameFilter of the window frames
+  kAlloc,      // newVideoFrame
+  kCopy,       // planes the filter does not process
+  kLock,       // waiting for the instance mutex
+  kForward,    // upload + forward launch of the frames entering the window
+  kProcess,    // filter + inverse + overlap-add launches and the readback
+  kPrune,      // spectra cache bookkeeping
+  kGpuFwd,     // device time: forward transform
+  kGpuFilter,  // the filter kernel (exact form: filter + inverse)
+  kGpuSynth,   // inverse + overlap-add + pack (exact form: overlap-add + pack)
+  kStages
+};
+const char* const kStageName[kStages] = {
+    "fetch source frames", "allocate output frame", "copy untouched planes", "wait for instance lock",
+    "upload + forward",    "filter .. readback",    "prune spectra cache",   "GPU: forward transform",
+    "GPU: filter",         "GPU: synthesis"};
+std::atomic<long long> g_stage_ns[kStages];
+std::atomic<long long> g_stage_calls[kStages];
+
+bool time_on() {
+  static const bool on = [] {
+    const char* p = std::getenv("FFT3DCL_TIME");
+    return p && *p;
+  }();
+  return on;
+}
+
+long long now_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+void add_stage(Stage s, long long ns) {
+  g_stage_ns[s] += ns;
+  g_stage_calls[s] += 1;
+}
+
+// Records the span from construction to destruction when timing is on.
+struct Span {
+  Stage s;
+  long long t0;
+  explicit Span(Stage st) : s(st), t0(time_on() ? now_ns() : 0) {}
+  ~Span() {
+    if (t0) add_stage(s, now_ns() - t0);
+  }
+};
+
+void dump_stages(const char* tag) {
+  if (!time_on()) return;
+  FILE* f = std::fopen(std::getenv("FFT3DCL_TIME"), "a");
+  if (!f) return;
+  std::fprintf(f, "== %s ==\n", tag);
+  long long total = 0;
+  for (int i = 0; i < kStages; i++) {
+    const long long ns = g_stage_ns[i].load(), calls = g_stage_calls[i].load();
+    if (i < kGpuFwd) total += ns;
+    std::fprintf(f, "  %-24s calls=%8lld  %9.4f s  %8.4f ms/call\n", kStageName[i], calls, ns / 1e9,
+                 calls ? ns / 1e6 / (double)calls : 0.0);
+  }
+  std::fprintf(f, "  %-24s %21.4f s\n", "host stages total", total / 1e9);
+  std::fclose(f);
+}
 
 struct Instance {
   f3d_script_params sp{};
@@ -88,9 +159,18 @@ const VSFrame* VS_CC get_frame(int n, int reason, void* data, void**, VSFrameCon
   }
   if (reason != arAllFramesReady) return nullptr;
 
-  const VSFrame* src = vsapi->getFrameFilter(n, in->clip, ctx);
-  VSFrame* dst = vsapi->newVideoFrame(&in->vi.format, in->vi.width, in->vi.height, src, core);
+  const VSFrame* src;
+  {
+    Span t(kFetch);
+    src = vsapi->getFrameFilter(n, in->clip, ctx);
+  }
+  VSFrame* dst;
+  {
+    Span t(kAlloc);
+    dst = vsapi->newVideoFrame(&in->vi.format, in->vi.width, in->vi.height, src, core);
+  }
   const int bps = in->vi.format.bytesPerSample;
+  const long long t_copy = time_on() ? now_ns() : 0;
   for (int p = 0; p < in->vi.format.numPlanes; p++) {  // untouched planes copied
     bool processed = false;
     for (int q : in->planes) processed |= q == p;
@@ -101,8 +181,11 @@ const VSFrame* VS_CC get_frame(int n, int reason, void* data, void**, VSFrameCon
     const int h = vsapi->getFrameHeight(src, p), row = vsapi->getFrameWidth(src, p) * bps;
     for (int y = 0; y < h; y++) std::memcpy(dp + y * ds, sp + y * ss, row);
   }
+  if (t_copy) add_stage(kCopy, now_ns() - t_copy);
 
+  const long long t_lock = time_on() ? now_ns() : 0;
   std::lock_guard<std::mutex> lock(in->mtx);
+  if (t_lock) add_stage(kLock, now_ns() - t_lock);
   for (size_t k = 0; k < in->planes.size(); k++) {
     const int p = in->planes[k];
     f3d_engine* e = in->engines[k];
@@ -114,9 +197,16 @@ const VSFrame* VS_CC get_frame(int n, int reason, void* data, void**, VSFrameCon
     else
       window.push_back(clamp_frame(n, num));
     bool ok = true;
+    int forwards = 0;
     for (int fn : window) {
       if (f3d_has(e, fn)) continue;
-      const VSFrame* fr = vsapi->getFrameFilter(fn, in->clip, ctx);
+      const VSFrame* fr;
+      {
+        Span t(kFetch);
+        fr = vsapi->getFrameFilter(fn, in->clip, ctx);
+      }
+      Span t(kForward);
+      forwards++;
       const uint8_t* sp = vsapi->getReadPtr(fr, p);
       const ptrdiff_t ss = vsapi->getStride(fr, p);
       if ((size_t)ss == row) {
@@ -130,6 +220,7 @@ const VSFrame* VS_CC get_frame(int n, int reason, void* data, void**, VSFrameCon
       if (!ok) break;
     }
     if (ok) {
+      Span t(kProcess);
       uint8_t* dp = vsapi->getWritePtr(dst, p);
       const ptrdiff_t ds = vsapi->getStride(dst, p);
       if ((size_t)ds == row) {
@@ -148,6 +239,17 @@ const VSFrame* VS_CC get_frame(int n, int reason, void* data, void**, VSFrameCon
       vsapi->freeFrame(src);
       return nullptr;
     }
+    if (time_on()) {
+      // The readback has completed, so the engine's events are: the last
+      // forward (this frame's, when one ran) and this output's kernels.
+      float ms[3];
+      if (f3d_last_kernel_ms(e, ms) == F3D_OK) {
+        if (forwards > 0 && ms[0] >= 0.0f) add_stage(kGpuFwd, (long long)(ms[0] * 1e6));
+        if (ms[1] >= 0.0f) add_stage(kGpuFilter, (long long)(ms[1] * 1e6));
+        if (ms[2] >= 0.0f) add_stage(kGpuSynth, (long long)(ms[2] * 1e6));
+      }
+    }
+    Span t(kPrune);
     // src/fft3dcl.cpp:457-466. Kalman keeps only the current frame; the
     // reference never prunes there and its cache grows with the clip.
     if (ip.bm >= 2)
@@ -166,6 +268,7 @@ void VS_CC free_filter(void* data, VSCore* core, const VSAPI* vsapi) {
   vsapi->freeNode(in->clip);
   delete in;
   log_usage(core, vsapi, "released");
+  dump_stages("FFT3DCL instance released (process totals)");
 }
 
 void VS_CC create(const VSMap* inmap, VSMap* out, void*, VSCore* core, const VSAPI* vsapi) {

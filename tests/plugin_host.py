@@ -40,7 +40,7 @@ def plane_shapes(family: str, width: int, height: int) -> list[tuple[int, int]]:
 
 
 def run_clip(exe: str, workdir: str, planes: list[list[np.ndarray]], family: str, bits: int,
-             order: str = "forward", form: str | None = None, **args):
+             order: str = "forward", form: str | None = None, extra_env: dict | None = None, **args):
     """Filters a clip through the plugin under the mock host.
 
     planes[p][n] is plane p of frame n (uint8, uint16 or float32). Returns
@@ -64,6 +64,7 @@ def run_clip(exe: str, workdir: str, planes: list[list[np.ndarray]], family: str
     env.pop("FFT3DCL_FORM", None)
     if form:
         env["FFT3DCL_FORM"] = form
+    env.update(extra_env or {})
     out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env)
     assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
     report = json.loads(out.stdout.strip().splitlines()[-1])

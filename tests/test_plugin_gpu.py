@@ -157,3 +157,33 @@ def test_float_yuv_and_mode0(host, tmp_path):
     run_and_compare(host, tmp_path, [y, u, v], "yuv", 32, {0, 1, 2}, chroma_planes=(1, 2), plane=4, bt=2)
     run_and_compare(host, tmp_path, [y, u, v], "yuv", 32, {0, 1, 2}, chroma_planes=(1, 2), plane=4, bt=3,
                     mode=0, bw=16, bh=16)
+
+
+def test_stage_timing_table(host, tmp_path):
+    # FFT3DCL_TIME (src/timing.h:1-31, timing.cpp:45-62): the released
+    # instance appends one line per stage with its calls and seconds; the
+    # output is unchanged by the timing.
+    y = synth.clip_gray8(width=160, height=96, frames=6)
+    path = tmp_path / "stages.txt"
+    out, rep = plugin_host.run_clip(host, str(tmp_path), [y], "gray", 8, form="tc", bt=3,
+                                    extra_env={"FFT3DCL_TIME": str(path)})
+    check_protocol(rep, 6)
+    plain, _ = plugin_host.run_clip(host, str(tmp_path), [y], "gray", 8, form="tc", bt=3)
+    assert all(np.array_equal(a, b) for a, b in zip(out[0], plain[0]))
+    lines = path.read_text().splitlines()
+    assert lines[0].startswith("== FFT3DCL")
+    calls = {}
+    for ln in lines[1:]:
+        if "calls=" in ln:
+            name, rest = ln.split("calls=")
+            calls[name.strip()] = int(rest.split()[0])
+    assert len(calls) == 10
+    # Six outputs: one source fetch each plus one per forwarded frame (every
+    # frame once), six output frames, six filter/synthesis kernel pairs.
+    assert calls["allocate output frame"] == 6
+    assert calls["upload + forward"] == 6
+    assert calls["fetch source frames"] == 12
+    assert calls["filter .. readback"] == 6
+    assert calls["GPU: filter"] == calls["GPU: synthesis"] == 6
+    assert 1 <= calls["GPU: forward transform"] <= 6
+    assert "host stages total" in lines[-1]
