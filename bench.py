@@ -390,6 +390,42 @@ def yuv_batched(args, dev, local_rank, peak):
     return res
 
 
+SECTIONS = ("yuv1080p_all_planes", "gray8_640x360_bt3", "grays_1280x720_kalman_bw64")
+
+
+def extra_section(name, args, dev, local_rank, peak):
+    """One of the workloads measured beside the headline (the other
+    configurations of the path), by name."""
+    from fft3dcl_gb300 import synth
+    if name == "yuv1080p_all_planes":
+        return dict(workload="1920x1080 YUV420P8 all planes, sigma=2.5 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4 "
+                             "scutoff=0.3 svr=1 smin=4 smax=20 degrid=1, clip resident in HBM",
+                    **yuv_batched(args, dev, local_rank, peak))
+    if name == "gray8_640x360_bt3":
+        return dict(workload="640x360 GRAY8, 16-frame clip, sigma=2 beta=1 bt=3 bw=bh=32 ow=oh=16 degrid=1 "
+                             "sharpen=0 (the plain method), clip resident in HBM",
+                    **config_section(args, dev, local_rank, synth.clip_gray8(), 8, GRAY8_PARAMS,
+                                     ("exact", "fast", "tc"), AB_GRAY8, peak, kbatch=16))
+    if name == "grays_1280x720_kalman_bw64":
+        return dict(workload="1280x720 GRAYS float, 64-frame clip with scene cuts at 20 and 45, Kalman bt=0 "
+                             "kratio=2 bw=bh=64 ow=oh=32, sigma pattern 2/1.5/2.5/3, state resident in HBM "
+                             "(Kalman runs the exact form in every form)",
+                    **config_section(args, dev, local_rank, synth.clip_grays(), 32, KALMAN_PARAMS, ("exact",),
+                                     AB_KALMAN, peak))
+    raise ValueError(f"unknown section {name}")
+
+
+def run_section(args, local_rank):
+    """--section NAME: that workload alone, one JSON line (for profiling
+    captures of its kernels)."""
+    import torch
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    peak, _ = load_peaks()
+    print(json.dumps({"section": args.section, **extra_section(args.section, args, dev, local_rank, peak)}),
+          flush=True)
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path on the host cores. The
     reference sources compile only here, so on the GPU host this is the C
@@ -719,22 +755,10 @@ def run_gpu(args, rank, world, local_rank):
         "gpu_launches": int(launches), "clocks": clk,
     }
     if world == 1 and not args.no_yuv:
-        line["yuv1080p_all_planes"] = dict(
-            workload="1920x1080 YUV420P8 all planes, sigma=2.5 bt=4 bw=bh=32 ow=oh=16 sharpen=0.4 scutoff=0.3 "
-                     "svr=1 smin=4 smax=20 degrid=1, clip resident in HBM", **yuv_batched(args, dev, local_rank, peak))
+        line["yuv1080p_all_planes"] = extra_section("yuv1080p_all_planes", args, dev, local_rank, peak)
     if world == 1 and not args.no_configs:
-        from fft3dcl_gb300 import synth
-        line["gray8_640x360_bt3"] = dict(
-            workload="640x360 GRAY8, 16-frame clip, sigma=2 beta=1 bt=3 bw=bh=32 ow=oh=16 degrid=1 sharpen=0 "
-                     "(the plain method), clip resident in HBM",
-            **config_section(args, dev, local_rank, synth.clip_gray8(), 8, GRAY8_PARAMS, ("exact", "fast", "tc"),
-                             AB_GRAY8, peak, kbatch=16))
-        line["grays_1280x720_kalman_bw64"] = dict(
-            workload="1280x720 GRAYS float, 64-frame clip with scene cuts at 20 and 45, Kalman bt=0 kratio=2 "
-                     "bw=bh=64 ow=oh=32, sigma pattern 2/1.5/2.5/3, state resident in HBM (Kalman runs the exact "
-                     "form in every form)",
-            **config_section(args, dev, local_rank, synth.clip_grays(), 32, KALMAN_PARAMS, ("exact",), AB_KALMAN,
-                             peak))
+        for name in ("gray8_640x360_bt3", "grays_1280x720_kalman_bw64"):
+            line[name] = extra_section(name, args, dev, local_rank, peak)
     if world == 1 and args.serve_streams > 0:
         # The serving workload: YUV 4:2:0 video streams (all planes) with
         # Poisson frame arrivals through the serving loop (shared steps for
@@ -826,6 +850,8 @@ def main():
     ap.add_argument("--serve-frames", type=int, default=120, help="frames per serving stream")
     ap.add_argument("--frames", type=int, default=NFRAMES,
                     help="frames of the resident clip (fewer only to keep profiler captures small)")
+    ap.add_argument("--section", default=None, choices=SECTIONS,
+                    help="run only this workload of the extra sections and print its results")
     args = ap.parse_args()
     if args.size:
         global W, H, WORKLOAD
@@ -837,6 +863,9 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
+        return
+    if args.section:
+        run_section(args, local_rank)
         return
     if world > 1:
         import torch.distributed as dist
