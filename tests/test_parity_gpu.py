@@ -76,6 +76,10 @@ def test_forward_spectra_exact(bw, bh):
     (32, 32, 3, {}), (16, 16, 4, {"sharpen": 0.5}), (64, 64, 1, {}), (8, 16, 2, {"degrid": 0.7}),
     (64, 32, 0, {"sigma2": 3.0}), (4, 4, -1, {"sharpen": 0.3}), (32, 64, 4, {"wintype": 1}),
     (16, 8, 3, {"ow": 4, "oh": 2}), (32, 16, 3, {"mode": 0}),
+    # 64 x 64 blocks run their transforms on lane pairs: every temporal mode
+    # family, sharpen, pattern, window types, mode 0.
+    (64, 64, 4, {"sharpen": 0.4, "sigma2": 2.5}), (64, 64, 3, {"mode": 0}),
+    (64, 64, 2, {"wintype": 2, "degrid": 0.5}), (64, 64, -1, {"sharpen": 0.2, "wintype": 1}),
 ])
 def test_block_sizes_and_modes_exact(bw, bh, bt, extra):
     frames = synth.moving_rects(150, 90, 6, bw + bh + bt, lo=16, hi=235, noise=4.0, n_rects=6)
