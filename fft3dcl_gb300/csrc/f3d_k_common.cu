@@ -37,13 +37,28 @@ __global__ void __launch_bounds__(256) k_ola(const __grid_constant__ OlaArgs a) 
     if (m0 < 0) m0 = 0;
     if (n1 > g.ncols - 1) n1 = g.ncols - 1;
     if (m1 > g.nrows - 1) m1 = g.nrows - 1;
-    for (int m = m0; m <= m1; m++) {
+    // The step is at least half the block (the overlap is at most half of
+    // it), so at most 2 x 2 blocks cover a sample: their values are loaded
+    // together, then added in block order.
+    float v[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+      const int m = m0 + i;
+      if (m > m1) continue;
       const int ly = y - (g.yoff + m * g.ystep);
-      for (int n = n0; n <= n1; n++) {
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const int n = n0 + j;
+        if (n > n1) continue;
         const int lx = x - (g.xoff + n * g.xstep);
-        sum += a.blocks[(size_t)(m * g.ncols + n) * bsz + ly * g.bw + lx];
+        v[i][j] = a.blocks[(size_t)(m * g.ncols + n) * bsz + ly * g.bw + lx];
       }
     }
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+      for (int j = 0; j < 2; j++)
+        if (m0 + i <= m1 && n0 + j <= n1) sum += v[i][j];
   } else {
     const int per = g.ncols * g.nrows;
     for (int grid = 0; grid < 2; grid++) {
