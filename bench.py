@@ -274,6 +274,7 @@ def config_section(args, dev, local_rank, frames, bits, params, forms, ab_bytes,
         if batch is not None:
             res[key]["how"] = (f"batch steps of {k} consecutive outputs, the next step's frames forwarded "
                                "concurrently, CUDA graph replay, autotuned launch shape")
+            res[key]["tune"] = batch.tune()
             batch.close()
         eng.close()
     if not args.no_cpu:

@@ -147,7 +147,23 @@ __global__ void __launch_bounds__(Cfg<BW, BH>::THREADS)
     }
   } else if (valid) {
     const size_t base = (size_t)b * C::PS;
-    for (int i = t; i < C::PS; i += C::TPB) F[i] = filter_bin(a, b, i, base + i);
+    const float dc = block_dc(a, b);
+    const KState none{make_float2(0.0f, 0.0f), 0.0f, 0.0f};
+    constexpr int KN = 4;  // bins whose window spectra are loaded together
+    for (int j0 = 0; j0 < C::NJ; j0 += KN) {
+      float2 sv[KN][4];
+#pragma unroll
+      for (int u = 0; u < KN; u++) {
+        const int i = t + (j0 + u) * C::TPB;
+        if (j0 + u < C::NJ && i < C::PS) load_window<kRuntimeBm>(a, base + i, sv[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < KN; u++) {
+        const int i = t + (j0 + u) * C::TPB;
+        if (j0 + u >= C::NJ || i >= C::PS) continue;
+        F[i] = filter_vals_ks<kRuntimeBm>(a, dc, bin_tables(a, i), base + i, sv[u], none);
+      }
+    }
   }
   __syncthreads();
   if (valid) {
