@@ -254,7 +254,8 @@ def config_section(args, dev, local_rank, frames, bits, params, forms, ab_bytes,
                 eng.prune(n - cur - 1, n + 2 * k - 1 - cur + need)
 
         n = max(cur, 1)
-        for _ in range(max(3, args.warmup)):
+        # Batches: the autotuner's step and the graph capture come first.
+        for _ in range(max(3 if batch is None else 6, args.warmup)):
             step(n)
             n += k
         torch.cuda.synchronize(dev)
