@@ -308,8 +308,9 @@ def yuv_batched(args, dev, local_rank, peak):
     bt, cur = ip.bt, ip.current
     res = {}
     # name: (form, storage flags, frames per step)
-    variants = {"tc": ("tc", 0, 1), "tc_4frames": ("tc", 0, 4), "tc_half": ("tc", F.FLAG_HALF_SPECTRA, 1),
-                "tc_half_4frames": ("tc", F.FLAG_HALF_SPECTRA, 4), "fast": ("fast", 0, 1)}
+    variants = {"tc": ("tc", 0, 1), "tc_4frames": ("tc", 0, 4), "tc_5frames": ("tc", 0, 5),
+                "tc_half": ("tc", F.FLAG_HALF_SPECTRA, 1), "tc_half_4frames": ("tc", F.FLAG_HALF_SPECTRA, 4),
+                "fast": ("fast", 0, 1)}
     for name, (form, flags, k) in variants.items():
         st = torch.cuda.Stream(device=dev)
         engs = [F.Engine(p[0].shape[1], p[0].shape[0], 8, chroma=i > 0, form=form, device=local_rank,
@@ -344,7 +345,7 @@ def yuv_batched(args, dev, local_rank, peak):
                 e.prune(n - cur - 1, n + k - 1 - cur + bt + k)
 
         n = cur
-        for _ in range(max(3, args.warmup)):
+        for _ in range(max(3 if batch is None else 6, args.warmup)):
             step(n)
             n += k
         torch.cuda.synchronize(dev)
@@ -372,6 +373,7 @@ def yuv_batched(args, dev, local_rank, peak):
                          "concurrent with the outputs")
     res["tc_4frames"]["form"] = ("as tc, four consecutive frames per step: 12 planes per launch "
                                  "([Y x4, U x4, V x4]; each plane's outputs share window spectra in L2)")
+    res["tc_5frames"]["form"] = "as tc_4frames with five consecutive frames per step: 15 planes per launch"
     res["tc_half"]["form"] = ("as tc, spectra cached as fp16 pairs (F3D_FLAG_HALF_SPECTRA: the original's "
                               "storage at precision 0, the default; opt-in, within +-1 LSB of the fp32 path)")
     res["tc_half_4frames"]["form"] = "as tc_4frames with fp16 spectrum storage"
