@@ -16,11 +16,12 @@
 //    next output of every stream whose window frames have arrived. Streams
 //    that run the fused tensor-core form are grouped by the parameters their
 //    kernels take (block size, overlap, window, temporal mode, sample
-//    format); each group has one CUDA stream, and the ready outputs of a
-//    group go into one step: one launch per kernel for up to sixteen planes
-//    of any sizes. Groups run concurrently with each other, as do the other
-//    streams (fast or exact form, Kalman) on their own CUDA streams. Streams
-//    opened while others run join the next pass;
+//    format) into lanes of up to three streams (consecutive opens: the
+//    planes of a YUV stream); each lane has one CUDA stream, and the ready
+//    outputs of a lane go into one step: one launch per kernel for its
+//    planes of any sizes. Lanes run concurrently with each other, as do the
+//    other streams (fast or exact form, Kalman) on their own CUDA streams.
+//    Streams opened while others run join the next pass;
 //  - latency: an output's latency runs from the arrival of the last input
 //    frame its window needs to the completion of its readback to host memory.
 #include "f3d_engine_internal.hpp"
@@ -67,6 +68,9 @@ constexpr int kOutSlots = 3;  // outputs a stream may hold before they are polle
 // measured 1-2% lower capacity and a higher server-side p99 on the bench's
 // serving mix).
 constexpr int kMaxInflight = 1;
+// Streams per lane: the three planes of a YUV stream share steps; streams of
+// different lanes run concurrently.
+constexpr int kLaneStreams = 3;
 
 struct InSlot {
   uint8_t* host = nullptr;  // pinned
@@ -91,7 +95,7 @@ struct Stream {
   cudaStream_t cs = nullptr;  // the stream's own CUDA stream, or its group's (batched)
   bool own_cs = true;
   bool batched = false;       // launched in shared steps with other streams
-  uint64_t gkey = 0;          // group of a batched stream
+  uint64_t gkey = 0;          // lane of a batched stream: launch key | lane index << 56
   // A batched stream copies on its own two CUDA streams, so that its copies
   // overlap its group's steps: the upload waits for the step that last read
   // the staging plane (ev_read), the step waits for the upload (ev_up) and
@@ -147,11 +151,13 @@ bool predict_batchable(int form, const f3d_internal_params& ip) {
 
 struct f3d_server {
   f3d_server_config cfg{};
-  // Groups of batched streams: one CUDA stream each, and the end events of
-  // the shared steps queued on it.
+  // Lanes of batched streams, by launch key and lane index: one CUDA
+  // stream each, the end events of the shared steps queued on it, and the
+  // open streams it holds.
   struct Group {
     cudaStream_t cs = nullptr;
     std::deque<cudaEvent_t> inflight;
+    int members = 0;
   };
   std::map<uint64_t, Group> groups;
   std::deque<cudaEvent_t> spare;  // unused step events
@@ -239,9 +245,9 @@ void f3d_server::reap(Stream* s) {
   }
 }
 
-// One shared step per group of batched streams whose next outputs are ready
-// and whose kernels take the same parameters (at most sixteen streams a
-// step). Returns whether anything was launched.
+// One shared step per lane of batched streams whose next outputs are ready
+// (their kernels take the same parameters). Returns whether anything was
+// launched.
 bool f3d_server::launch_shared() {
   std::map<uint64_t, std::vector<Stream*>> ready_by_group;
   std::vector<int> win;
@@ -454,8 +460,17 @@ int f3d_server_open(f3d_server* sv, const f3d_script_params* sp, const f3d_plane
   if (rc != F3D_OK) return rc;
   auto s = std::unique_ptr<Stream, void (*)(Stream*)>(new Stream(), free_stream);
   if (predict_batchable(sv->cfg.form, ip)) {
-    s->gkey = f3d::plane_batch_key(ip, *geom);
+    const uint64_t key = f3d::plane_batch_key(ip, *geom);
     std::lock_guard<std::mutex> lk(sv->mtx);
+    // The first lane of this key with room (lanes are counted when a stream
+    // is registered below).
+    uint64_t lane = 0;
+    while (lane < 255) {
+      auto it = sv->groups.find(key | (lane << 56));
+      if (it == sv->groups.end() || it->second.members < kLaneStreams) break;
+      lane++;
+    }
+    s->gkey = key | (lane << 56);
     f3d_server::Group& g = sv->groups[s->gkey];
     if (!g.cs && cudaStreamCreateWithFlags(&g.cs, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
@@ -515,6 +530,7 @@ int f3d_server_open(f3d_server* sv, const f3d_script_params* sp, const f3d_plane
   }
   std::lock_guard<std::mutex> lk(sv->mtx);
   Stream* st = s.release();
+  if (st->batched || !st->own_cs) sv->groups[st->gkey].members++;
   st->id = sv->next_id++;
   *sid = st->id;
   sv->streams[st->id] = st;
@@ -600,6 +616,7 @@ int f3d_server_close(f3d_server* sv, int sid) {
     s = it->second;
     sv->streams.erase(it);
     sv->used_bytes -= s->est_bytes;
+    if (!s->own_cs) sv->groups[s->gkey].members--;
   }
   free_stream(s);
   sv->work_cv.notify_all();

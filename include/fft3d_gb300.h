@@ -309,12 +309,13 @@ int f3d_batch_last_kernel_ms(f3d_batch* b, float* ms);
  * streams fits `hbm_budget` and fewer than `max_streams` are open; otherwise
  * f3d_server_open returns F3D_E_BUSY. On every pass the scheduler launches
  * the next output of every stream whose window frames have arrived. Streams
- * whose engines run the fused tensor-core form share one CUDA stream, and
- * their ready outputs go into shared steps: one launch per kernel for up to
- * sixteen streams whose kernels take the same parameters (block size,
- * overlap, window, temporal mode, sample format), planes of any size. The
- * other streams launch on their own CUDA streams, so their kernels overlap
- * on the device. Streams that open while others run join at once. Latency of
+ * whose engines run the fused tensor-core form and whose kernels take the
+ * same parameters (block size, overlap, window, temporal mode, sample
+ * format) form lanes of up to three streams in the order they open (the
+ * planes of a YUV stream); each lane has one CUDA stream, and its ready
+ * outputs go into shared steps: one launch per kernel for its planes of any
+ * size. Lanes and the other streams (on CUDA streams of their own) run
+ * concurrently on the device. Streams that open while others run join at once. Latency of
  * an output: from the arrival of the last input frame its window needs to
  * the end of its copy to host memory. A video stream of several planes (YUV)
  * is one server stream per plane. */
