@@ -21,6 +21,7 @@ replica on its own GPU (the path does not shard across GPUs).
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -680,6 +681,7 @@ def run_gpu(args, rank, world, local_rank):
     barrier()
     torch.cuda.synchronize(dev)
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gc.disable()  # no collector pause inside the host-driven timed loop
     h0.record(stream)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -690,6 +692,7 @@ def run_gpu(args, rank, world, local_rank):
     h1.record(stream)
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t0
+    gc.enable()
     barrier()
     ms_e2e = max(h0.elapsed_time(h1), wall * 1000.0)
     if batched:
