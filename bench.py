@@ -794,7 +794,8 @@ def run_gpu(args, rank, world, local_rank):
                     "p99_ms": round(st["p99_ms"], 3), "server_p99_ms": round(st["server_p99_ms"], 3),
                     "submit_lag_p99_ms": round(st["submit_lag_p99_ms"], 3),
                     "shared_steps": st["shared_steps"], "outputs_per_shared_step":
-                        round(st["shared_outputs"] / st["shared_steps"], 2) if st["shared_steps"] else None}
+                        round(st["shared_outputs"] / st["shared_steps"], 2) if st["shared_steps"] else None,
+                    "scheduler_busy": round(st["scheduler_busy"], 3) if st["scheduler_busy"] is not None else None}
 
         st = serve(1.0)
         sweep = [point(1.0, st)]

@@ -177,7 +177,7 @@ class ServerStats(C.Structure):
     _fields_ = [("frames", C.c_longlong), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("max_ms", C.c_double), ("mean_ms", C.c_double), ("seconds", C.c_double),
                 ("open_streams", C.c_int), ("used_bytes", C.c_size_t), ("shared_steps", C.c_longlong),
-                ("shared_outputs", C.c_longlong), ("max_shared", C.c_int)]
+                ("shared_outputs", C.c_longlong), ("max_shared", C.c_int), ("busy_ms", C.c_double)]
 
 
 F3D_E_BUSY = -6

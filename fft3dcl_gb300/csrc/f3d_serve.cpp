@@ -162,6 +162,7 @@ struct f3d_server {
   std::map<uint64_t, Group> groups;
   std::deque<cudaEvent_t> spare;  // unused step events
   long long steps = 0, step_outputs = 0;
+  double busy_ms = 0.0;  // scheduler passes that launched work
   int max_step = 0;
   std::mutex mtx;
   std::condition_variable work_cv, done_cv;
@@ -386,6 +387,7 @@ void f3d_server::run() {
   std::unique_lock<std::mutex> lk(mtx);
   while (!stop) {
     bool any = false, pending = false;
+    const double t_pass = now_ms();
     for (auto& kv : streams) {
       Stream* s = kv.second;
       reap(s);
@@ -402,6 +404,7 @@ void f3d_server::run() {
     for (int k = 0; k < kOutSlots && launch_shared(); k++) any = true;
     for (auto& kv : streams)
       for (OutSlot* o : kv.second->outs) pending |= !o->done;
+    if (any) busy_ms += now_ms() - t_pass;
     done_cv.notify_all();
     if (!any) {
       // In-flight outputs are polled every 50 us; otherwise sleep until a
@@ -634,6 +637,7 @@ int f3d_server_get_stats(f3d_server* sv, f3d_server_stats* st) {
   st->shared_steps = sv->steps;
   st->shared_outputs = sv->step_outputs;
   st->max_shared = sv->max_step;
+  st->busy_ms = sv->busy_ms;
   if (v.empty()) return F3D_OK;
   std::sort(v.begin(), v.end());
   auto pct = [&](double q) { return v[std::min(v.size() - 1, (size_t)(q * (v.size() - 1) + 0.5))]; };

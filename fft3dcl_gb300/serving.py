@@ -223,5 +223,6 @@ def run(server: Server, specs: list[dict], frames: list[list[list[np.ndarray]]],
         p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)), max_ms=float(lat.max()),
         server_p50_ms=float(np.percentile(lat_srv, 50)), server_p99_ms=float(np.percentile(lat_srv, 99)),
         submit_lag_p99_ms=float(np.percentile(lag, 99)) if realtime else None,
-        plane_p50_ms=st["p50_ms"], plane_p99_ms=st["p99_ms"])
+        plane_p50_ms=st["p50_ms"], plane_p99_ms=st["p99_ms"],
+        scheduler_busy=st["busy_ms"] / 1000.0 / seconds if seconds > 0 else None)
     return [r["outs"] for r in res], st

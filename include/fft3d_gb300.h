@@ -335,6 +335,7 @@ typedef struct {
   long long shared_steps;   /* steps launched for several streams at once */
   long long shared_outputs; /* outputs of those steps */
   int max_shared;           /* most outputs in one shared step */
+  double busy_ms;           /* scheduler thread: time spent in passes that launched work */
 } f3d_server_stats;
 
 typedef struct f3d_server f3d_server;
