@@ -147,6 +147,89 @@ bool predict_batchable(int form, const f3d_internal_params& ip) {
          ip.oh * 2 == ip.bh;
 }
 
+// Host copies of large planes (a submitted frame into its pinned slot, a
+// finished output out of its slot) split by rows over a few helper threads
+// and the calling thread, so that a 4K frame's copy is not one core's
+// memory bandwidth.
+class CopyPool {
+ public:
+  explicit CopyPool(int helpers) {
+    for (int i = 0; i < helpers; i++) th_.emplace_back([this] { loop(); });
+  }
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> lk(mtx_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  // Rows [0, h) of `row` bytes from src (pitch sp) to dst (pitch dp).
+  void copy_rows(uint8_t* dst, long long dp, const uint8_t* src, long long sp, int h, size_t row) {
+    const int parts = row * h < kSplitBytes ? 1 : std::min((int)th_.size() + 1, h);
+    if (parts <= 1) {
+      rows(dst, dp, src, sp, 0, h, row);
+      return;
+    }
+    std::mutex m;
+    std::condition_variable done;
+    int left = parts - 1;
+    {
+      std::lock_guard<std::mutex> lk(mtx_);
+      for (int p = 1; p < parts; p++)
+        jobs_.push_back(Job{dst, dp, src, sp, (int)((long long)h * p / parts), (int)((long long)h * (p + 1) / parts),
+                            row, &left, &m, &done});
+    }
+    cv_.notify_all();
+    rows(dst, dp, src, sp, 0, h / parts, row);
+    std::unique_lock<std::mutex> lk(m);
+    done.wait(lk, [&] { return left == 0; });
+  }
+
+ private:
+  static constexpr size_t kSplitBytes = 1 << 20;
+  struct Job {
+    uint8_t* dst;
+    long long dp;
+    const uint8_t* src;
+    long long sp;
+    int y0, y1;
+    size_t row;
+    int* left;
+    std::mutex* m;
+    std::condition_variable* done;
+  };
+  static void rows(uint8_t* dst, long long dp, const uint8_t* src, long long sp, int y0, int y1, size_t row) {
+    if (dp == (long long)row && sp == (long long)row) {
+      std::memcpy(dst + (size_t)y0 * row, src + (size_t)y0 * row, (size_t)(y1 - y0) * row);
+      return;
+    }
+    for (int y = y0; y < y1; y++) std::memcpy(dst + y * dp, src + y * sp, row);
+  }
+  void loop() {
+    for (;;) {
+      Job j;
+      {
+        std::unique_lock<std::mutex> lk(mtx_);
+        cv_.wait(lk, [&] { return stop_ || !jobs_.empty(); });
+        if (jobs_.empty()) return;  // stop_
+        j = jobs_.front();
+        jobs_.pop_front();
+      }
+      rows(j.dst, j.dp, j.src, j.sp, j.y0, j.y1, j.row);
+      // The caller's mutex is held while its counter drops and it is woken,
+      // so the caller cannot return (and free both) before this is done.
+      std::lock_guard<std::mutex> g(*j.m);
+      if (--*j.left == 0) j.done->notify_all();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex mtx_;
+  std::condition_variable cv_;
+  std::deque<Job> jobs_;
+  bool stop_ = false;
+};
+
 }  // namespace
 
 struct f3d_server {
@@ -173,6 +256,7 @@ struct f3d_server {
   double t_first = -1.0, t_last = 0.0;
   std::atomic<bool> stop{false};
   std::thread worker;
+  CopyPool copies{3};
 
   void run();
   bool ready(Stream* s, int n, std::vector<int>& win);
@@ -561,8 +645,8 @@ int f3d_server_submit(f3d_server* sv, int sid, int n, const void* src, long long
     slot->state = InSlot::RESERVED;  // held while the copy below runs
     slot->frame = -1;
   }
-  const uint8_t* p = static_cast<const uint8_t*>(src);
-  for (int y = 0; y < s->H; y++) std::memcpy(slot->host + y * s->row_bytes, p + y * pitch, s->row_bytes);
+  sv->copies.copy_rows(slot->host, (long long)s->row_bytes, static_cast<const uint8_t*>(src), pitch, s->H,
+                       s->row_bytes);
   {
     std::lock_guard<std::mutex> lk(sv->mtx);
     slot->frame = n;
@@ -598,10 +682,8 @@ int f3d_server_poll_timed(f3d_server* sv, int sid, int* n, void* dst, long long 
   // launching meanwhile; the slot stays busy (not reused) until it is done.
   // One thread polls a stream.
   lk.unlock();
-  if (dst) {
-    uint8_t* d = static_cast<uint8_t*>(dst);
-    for (int y = 0; y < s->H; y++) std::memcpy(d + y * pitch, o->host + y * s->row_bytes, s->row_bytes);
-  }
+  if (dst)
+    sv->copies.copy_rows(static_cast<uint8_t*>(dst), pitch, o->host, (long long)s->row_bytes, s->H, s->row_bytes);
   lk.lock();
   s->outs.pop_front();
   o->busy = false;
