@@ -81,6 +81,8 @@ def test_shared_steps_all_at_once():
         outs, st = serving.run(sv, specs, frames, realtime=False, timeout_s=120)
     assert st["max_shared"] >= 2, st
     assert st["shared_outputs"] == st["frames"]
+    # The scheduler's launching passes are part of the run.
+    assert 0.0 < st["scheduler_busy"] <= 1.0, st
     for spec, fr, got in zip(specs, frames, outs):
         for gp, rp in zip(got, alone(spec, fr, "tc")):
             for g, r in zip(gp, rp):
