@@ -431,6 +431,50 @@ def run_section(args, local_rank):
           flush=True)
 
 
+def fast_batch_run(args, dev, local_rank, clip_dev, k):
+    """Steady-state batch steps of k consecutive outputs in the fast form,
+    the clip resident in HBM, the frames after the windows forwarded in the
+    same step (concurrently with the sweeps)."""
+    import torch
+    import fft3dcl_gb300 as F
+    ip = F.validate(W, H, BITS, **PARAMS)
+    bt, cur = ip.bt, ip.current
+    pitch, nfr = W * 2, clip_dev.shape[0]
+    stream = torch.cuda.Stream(device=dev)
+    eng = F.Engine(W, H, BITS, form="fast", device=local_rank, stream=stream.cuda_stream, **PARAMS)
+    outs = [torch.empty((H, W), dtype=torch.uint16, device=dev) for _ in range(k)]
+    batch = F.Batch([eng] * k, graph=False, autotune=False)
+
+    def step(n):
+        wins = [[m - cur + i for i in range(bt)] for m in range(n, n + k)]
+        for w in wins:
+            for fn in w:
+                if not eng.has(fn):
+                    eng.forward_device(fn, clip_dev[fn % nfr].data_ptr(), pitch)
+        ahead = [n + k - 1 - cur + bt + i for i in range(k)]
+        batch.step(ahead, [clip_dev[a % nfr].data_ptr() for a in ahead], [pitch] * k, wins,
+                   [o.data_ptr() for o in outs], [pitch] * k)
+        eng.prune(n - cur - 1, n + k - 1 - cur + bt + k)
+
+    n = cur
+    for _ in range(max(3, args.warmup)):
+        step(n)
+        n += k
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(n)
+        n += k
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    fps = args.steps * k / (e0.elapsed_time(e1) / 1000.0)
+    batch.close()
+    eng.close()
+    return {"value": round(fps, 3), "how": f"batch steps of {k} consecutive outputs: one forward launch per entering "
+                                          "frame, the fused sweeps of the outputs in one launch, no graph"}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path on the host cores. The
     reference sources compile only here, so on the GPU host this is the C
@@ -594,6 +638,11 @@ def run_gpu(args, rank, world, local_rank):
                     "kernel_ms": [round(float(x), 4) for x in kt_f]}
         eng_f.close()
     batched = args.form == "tc" and not args.no_batch
+    if batched and "fast" in args.compare.split(","):
+        # The plain form batched the same way: k consecutive outputs per step
+        # (one forward launch per entering frame, the k fused sweeps in one
+        # launch with their CTAs interleaved), launched directly.
+        forms["fast_batch"] = fast_batch_run(args, dev, local_rank, clip_dev, kout)
     if batched:
         # The tensor-core engine's own calls, for comparison with its batch.
         ms_d, kt_d, _, _, eng_d, _, _, _ = device_run("tc")

@@ -608,10 +608,11 @@ BATCH_AUTOTUNE = 2
 
 
 class Batch:
-    """One temporal step of up to sixteen tensor-core engines (the planes of a
-    frame, planes of several streams, or one engine several times for
-    consecutive outputs) with one launch per kernel
-    (f3d_batch_*); optionally replayed as a CUDA graph and autotuned."""
+    """One temporal step of up to sixteen tensor-core engines, or fast-form
+    engines (the planes of a frame, planes of several streams, or one engine
+    several times for consecutive outputs) with one launch per kernel
+    (f3d_batch_*; the fast form: one forward launch per entering frame);
+    tensor-core batches optionally replayed as a CUDA graph and autotuned."""
 
     def __init__(self, engines: list, graph: bool = True, autotune: bool = True):
         self.engines = list(engines)

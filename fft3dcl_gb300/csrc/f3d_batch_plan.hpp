@@ -33,14 +33,20 @@ inline bool forward_batch(const TcFwdArgs* planes, int n, TcFwdBatch& B) {
 
 // The three sweep-side batch parameters (filter, inverse, seam merge) of
 // `planes`: the same planes, with the prefix of each kernel's CTA counts.
-inline bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& Bs, SweepBatch& Bm) {
+// tc: the tensor-core sweep (16x16 or 32x32 blocks, tables, operand tiles);
+// otherwise the fast form's fused sweep (8x8 to 32x32 blocks; only Bs and Bm
+// are used).
+inline bool sweep_batches(const SweepArgs* planes, int n, SweepBatch& Bf, SweepBatch& Bs, SweepBatch& Bm,
+                          bool tc = true) {
   if (n < 1 || n > kMaxBatch) return false;
   SweepBatch B{};
   B.n = n;
   for (int i = 0; i < n; i++) {
     const SweepArgs& a = planes[i];
-    if ((a.inv.g.bw != 16 && a.inv.g.bw != 32) || a.inv.g.bh != a.inv.g.bw || a.inv.g.bw != planes[0].inv.g.bw ||
-        !a.tab || !a.err || !a.img || a.inv.bm != planes[0].inv.bm || a.inv.half != planes[0].inv.half)
+    const int bw = a.inv.g.bw;
+    const bool size_ok = tc ? (bw == 16 || bw == 32) : (bw == 8 || bw == 16 || bw == 32);
+    if (!size_ok || a.inv.g.bh != bw || bw != planes[0].inv.g.bw || (tc && (!a.tab || !a.err || !a.img)) ||
+        a.inv.bm != planes[0].inv.bm || a.inv.half != planes[0].inv.half)
       return false;
     B.p[i] = a;
   }

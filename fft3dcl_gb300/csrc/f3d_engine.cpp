@@ -214,9 +214,9 @@ TcFwdArgs tc_forward_args(const f3d_engine* e, const uint8_t* dsrc, long long pi
   return t;
 }
 
-int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int fmt) {
-  float2* spec = spectra_slot(e, fn, true);
-  if (!spec) return e->fail(F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
+// Forward arguments of the exact and fast forms for a frame whose spectra go
+// to `spec`.
+FwdArgs forward_args(const f3d_engine* e, const uint8_t* dsrc, long long pitch, int fmt, float2* spec) {
   FwdArgs a{};
   a.g = make_geo(e);
   a.tw = make_twiddles(e);
@@ -229,6 +229,13 @@ int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int
   a.spec = spec;
   a.twr = e->d_twr;
   a.twc = e->d_twc;
+  return a;
+}
+
+int run_forward(f3d_engine* e, int fn, const uint8_t* dsrc, long long pitch, int fmt) {
+  float2* spec = spectra_slot(e, fn, true);
+  if (!spec) return e->fail(F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
+  const FwdArgs a = forward_args(e, dsrc, pitch, fmt, spec);
   cudaEventRecord(e->ev[0], e->stream);
   cudaError_t ce;
   if (e->form == F3D_FORM_TC) {
@@ -830,6 +837,10 @@ struct f3d_batch {
   std::vector<uint8_t*> img;   // per entry, null: the engine's own
   std::vector<float*> seam;
   std::vector<size_t> img_bytes, seam_bytes;
+  std::vector<bool> repeat;    // per entry: its engine appeared earlier
+  // Fast-form engines: the forwards launch per entry, the fused sweeps of
+  // all entries as one launch; no graph, no launch shapes to tune.
+  bool fast = false;
 };
 
 namespace {
@@ -863,8 +874,12 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
   for (int i = 0; i < n; i++) {
     const f3d_engine* e = engines[i];
     if (!e) return fail_thread(F3D_E_PARAM, "FFT3DCL: null engine in batch");
-    if (e->form != F3D_FORM_TC || e->inv_form != F3D_FORM_TC || !e->fused)
-      return fail_thread(F3D_E_UNSUPPORTED, "FFT3DCL: batches run the fused tensor-core form");
+    const bool tc = e->form == F3D_FORM_TC && e->inv_form == F3D_FORM_TC && e->fused;
+    const bool fast = e->form == F3D_FORM_FAST && e->inv_form == F3D_FORM_FAST && e->fused;
+    if (!tc && !fast)
+      return fail_thread(F3D_E_UNSUPPORTED, "FFT3DCL: batches run the fused tensor-core or fast form");
+    if (e->form != e0->form)
+      return fail_thread(F3D_E_UNSUPPORTED, "FFT3DCL: the engines of a batch run one form");
     if (e->device != e0->device || e->stream != e0->stream)
       return fail_thread(F3D_E_PARAM, "FFT3DCL: the engines of a batch share one device and stream");
     if (e->ip.bw != e0->ip.bw || e->ip.bh != e0->ip.bh || e->ip.ow != e0->ip.ow || e->ip.oh != e0->ip.oh ||
@@ -881,6 +896,8 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
   b->seam.assign(n, nullptr);
   b->img_bytes.assign(n, 0);
   b->seam_bytes.assign(n, 0);
+  b->repeat.assign(n, false);
+  b->fast = e0->form == F3D_FORM_FAST;
   for (int i = 0; i < n; i++) {
     // An engine that appears k times enters k frames per step.
     int k = 0;
@@ -892,10 +909,11 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
     bool repeat = false;
     for (int j = 0; j < i; j++) repeat |= engines[j] == engines[i];
     if (!repeat) continue;
+    b->repeat[i] = true;
     const f3d_engine* e = engines[i];
-    b->img_bytes[i] = e->img_bytes;
+    b->img_bytes[i] = b->fast ? 0 : e->img_bytes;  // the fast sweep has no operand tiles
     b->seam_bytes[i] = sizeof(float) * e->seam_floats;
-    if (cudaMalloc(&b->img[i], b->img_bytes[i]) != cudaSuccess ||
+    if ((b->img_bytes[i] && cudaMalloc(&b->img[i], b->img_bytes[i]) != cudaSuccess) ||
         (b->seam_bytes[i] && cudaMalloc(&b->seam[i], b->seam_bytes[i]) != cudaSuccess)) {
       cudaGetLastError();
       f3d_batch_destroy(b);
@@ -957,6 +975,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   }
   cudaSetDevice(b->eng[0]->device);
   TcFwdArgs fa[kMaxBatch];
+  FwdArgs ff[kMaxBatch];  // fast form
   SweepArgs sa[kMaxBatch];
   int nf = 0;
   uint64_t mask = 0;
@@ -967,7 +986,10 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
         return batch_fail(b, F3D_E_PARAM, "FFT3DCL: bad source plane in batch");
       float2* spec = spectra_slot(e, fns[i], true);
       if (!spec) return batch_fail(b, F3D_E_NOMEM, "FFT3DCL: GPU spectra alloc failed");
-      fa[nf++] = tc_forward_args(e, static_cast<const uint8_t*>(dev_src[i]), (long long)src_pitch[i], e->fmt, spec);
+      const uint8_t* src = static_cast<const uint8_t*>(dev_src[i]);
+      if (b->fast) ff[nf] = forward_args(e, src, (long long)src_pitch[i], e->fmt, spec);
+      else fa[nf] = tc_forward_args(e, src, (long long)src_pitch[i], e->fmt, spec);
+      nf++;
       mask |= 1ull << i;
     }
   }
@@ -982,7 +1004,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
       return batch_fail(b, F3D_E_PARAM, "FFT3DCL: bad output plane in batch");
     sa[ns] = sweep_args(e, a, static_cast<uint8_t*>(dev_dst[i]), (long long)dst_pitch[i], e->fmt);
     e->test_skip = false;
-    if (b->img[i]) {  // a repeated engine: this output's own tiles and seam rows
+    if (b->repeat[i]) {  // a repeated engine: this output's own tiles and seam rows
       sa[ns].img = b->img[i];
       sa[ns].seam_b = b->seam[i];
       sa[ns].seam_t = b->seam[i] ? b->seam[i] + (size_t)(sa[ns].segs - 1) * (a.g.bh / 2) * sa[ns].seam_w : nullptr;
@@ -1010,24 +1032,42 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
     cudaStreamIsCapturing(b->stream, &cs);
     const bool timed = cs == cudaStreamCaptureStatusNone;
     if (timed) cudaEventRecord(b->kev[0], b->stream);
-    cudaError_t ce = launch_sweep_tc_batch(sa, ns, t, b->stream, timed ? b->kev[1] : nullptr, after_filter);
+    cudaError_t ce = b->fast ? launch_sweep_fast_batch(sa, ns, b->stream, timed ? b->kev[1] : nullptr)
+                             : launch_sweep_tc_batch(sa, ns, t, b->stream, timed ? b->kev[1] : nullptr, after_filter);
     if (timed && ce == cudaSuccess) {
       cudaEventRecord(b->kev[2], b->stream);
       b->ktimed = true;
     }
     return ce;
   };
+  auto forwards = [&](const TcTune& t, cudaStream_t st) -> cudaError_t {
+    if (!b->fast) return launch_forward_tc_batch(fa, nf, t, st);
+    for (int k = 0; k < nf; k++) {
+      const cudaError_t ce = launch_forward(F3D_FORM_FAST, ff[k], st);
+      if (ce != cudaSuccess) return ce;
+    }
+    return cudaSuccess;
+  };
   auto launch = [&](const TcTune& t) -> cudaError_t {
     cudaError_t ce = cudaSuccess;
+    if (overlap && b->fast) {  // the fused fast sweep has no filter-only part: fork at the start
+      ce = cudaEventRecord(b->fork, b->stream);
+      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
+      if (ce == cudaSuccess) ce = forwards(t, b->side);
+      if (ce == cudaSuccess) ce = cudaEventRecord(b->join, b->side);
+      if (ce == cudaSuccess) ce = sweep(t, nullptr);
+      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->stream, b->join, 0);
+      return ce;
+    }
     if (overlap) {
       ce = sweep(t, b->fork);
       if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->side, b->fork, 0);
-      if (ce == cudaSuccess) ce = launch_forward_tc_batch(fa, nf, t, b->side);
+      if (ce == cudaSuccess) ce = forwards(t, b->side);
       if (ce == cudaSuccess) ce = cudaEventRecord(b->join, b->side);
       if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->stream, b->join, 0);
       return ce;
     }
-    ce = nf ? launch_forward_tc_batch(fa, nf, t, b->stream) : cudaSuccess;
+    ce = nf ? forwards(t, b->stream) : cudaSuccess;
     if (ce == cudaSuccess && ns) ce = sweep(t, nullptr);
     return ce;
   };
@@ -1038,7 +1078,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
   // than 1 % slower: step-to-step noise of about 1 % picked a filter variant
   // 1-3 % slower in steady state at eight and ten outputs.
   const uint64_t all = (1ull << n) - 1;
-  if ((b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFFFFFull) == (all | (all << 16))) {
+  if (!b->fast && (b->flags & F3D_BATCH_AUTOTUNE) && !b->tuned && (mask & 0xFFFFFFFFull) == (all | (all << 16))) {
     const TcTune cands[] = {{3, 5}, {2, 5}, {1, 5}, {3, 4}, {2, 4}, {1, 4}, {3, 3}, {2, 3}, {1, 3}};
     constexpr int kCands = sizeof(cands) / sizeof(cands[0]);
     cudaEvent_t t0, t1;
@@ -1072,7 +1112,7 @@ int f3d_batch_step(f3d_batch* b, const int* fns, const void* const* dev_src, con
     return launch(b->tune) == cudaSuccess ? F3D_OK : batch_fail(b, F3D_E_CUDA, "FFT3DCL: batch launch failed");
   }
   cudaError_t ce = cudaSuccess;
-  if (b->flags & F3D_BATCH_GRAPH) {
+  if ((b->flags & F3D_BATCH_GRAPH) && !b->fast) {  // fast batches launch directly
     // One CUDA graph per batch shape, captured at its first step; later steps
     // re-point its kernel nodes at the step's buffers and replay it.
     auto it = b->graphs.find(mask);

@@ -25,7 +25,10 @@
 // spectra can be bulk-prefetched into L2 while row m is processed (off by
 // default: with one wave of CTAs each holding a row, the prefetched rows
 // exceed what L2 keeps and the extra traffic costs more than it hides).
+#include "f3d_batch_plan.hpp"
 #include "f3d_fast.cuh"
+
+#include <algorithm>
 
 namespace f3d {
 namespace {
@@ -78,8 +81,9 @@ __device__ __forceinline__ void store4(const SweepArgs& sa, int y, int x, float4
   }
 }
 
+// CTA `cta` (strip, segment) of plane sa's sweep.
 template <int BW, int BH, int BM>
-__global__ void __launch_bounds__(kSweepThreads, F3D_SWEEP_MINB) k_sweep_fast(const __grid_constant__ SweepArgs sa) {
+__device__ __forceinline__ void sweep_fast_cta(const SweepArgs& sa, int cta) {
   using S_ = SCfg<BW, BH>;
   using C = FCfg<BW, BH>;
   constexpr int TPB = S_::TPB, TJ = S_::TJ, CW = S_::CW, CH = S_::CH, QK = S_::QK;
@@ -90,7 +94,7 @@ __global__ void __launch_bounds__(kSweepThreads, F3D_SWEEP_MINB) k_sweep_fast(co
   float4* P = reinterpret_cast<float4*>(slots + S_::SLOTS * C::SMEM_F2);  // [TJ][CH][QK]
   const int slot = threadIdx.x / TPB, t = threadIdx.x - slot * TPB;
   float2* S = slots + slot * C::SMEM_F2;
-  const int strip = blockIdx.x % sa.strips, seg = blockIdx.x / sa.strips;
+  const int strip = cta % sa.strips, seg = cta / sa.strips;
   const int J0 = strip * TJ;
   const int nrow = sa.cells_y + 1;  // block rows 0..cells_y are needed
   const int M0 = (int)((long long)seg * nrow / sa.segs);
@@ -154,6 +158,24 @@ __global__ void __launch_bounds__(kSweepThreads, F3D_SWEEP_MINB) k_sweep_fast(co
   }
 }
 
+template <int BW, int BH, int BM>
+__global__ void __launch_bounds__(kSweepThreads, F3D_SWEEP_MINB) k_sweep_fast(const __grid_constant__ SweepArgs sa) {
+  sweep_fast_cta<BW, BH, BM>(sa, blockIdx.x);
+}
+
+// The sweeps of a batch of planes in one launch: the CTAs of a run of
+// planes of one geometry (consecutive outputs of a plane) are interleaved,
+// so that the window spectra they share are read from L2 the second time.
+template <int BW, int BH, int BM>
+__global__ void __launch_bounds__(kSweepThreads, F3D_SWEEP_MINB)
+    k_sweep_fast_batch(const __grid_constant__ SweepBatch B) {
+  int p = 0;
+  while (p + 1 < B.n && (int)blockIdx.x >= B.cta0[p + 1]) p++;
+  const int r0 = B.run[p], rl = B.rlen[r0];
+  const int local = (int)blockIdx.x - B.cta0[r0];
+  sweep_fast_cta<BW, BH, BM>(B.p[r0 + local % rl], local / rl);
+}
+
 // Finishes the seam cell rows: ((q1 + q2) + q3) + q4 per sample, packed.
 __global__ void __launch_bounds__(256) k_seam_merge(const __grid_constant__ SweepArgs sa, int ch) {
   const int x = blockIdx.x * 256 + threadIdx.x;
@@ -186,6 +208,30 @@ cudaError_t launch_bm(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
   return launch_seam_merge(a, st);
 }
 
+template <int BW, int BH, int BM>
+cudaError_t launch_batch_bm(const SweepBatch& Bs, int n, cudaStream_t st) {
+  using S_ = SCfg<BW, BH>;
+  auto k = k_sweep_fast_batch<BW, BH, BM>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_::SMEM);
+  if (e != cudaSuccess) return e;
+  if (Bs.cta0[n] == 0) return cudaSuccess;
+  k<<<Bs.cta0[n], kSweepThreads, S_::SMEM, st>>>(Bs);
+  count_launch();
+  return cudaGetLastError();
+}
+
+template <int BW, int BH>
+cudaError_t launch_batch_size(const SweepBatch& Bs, int n, cudaStream_t st) {
+  switch (Bs.p[0].inv.bm) {
+  case -1: return launch_batch_bm<BW, BH, -1>(Bs, n, st);
+  case 1: return launch_batch_bm<BW, BH, 1>(Bs, n, st);
+  case 2: return launch_batch_bm<BW, BH, 2>(Bs, n, st);
+  case 3: return launch_batch_bm<BW, BH, 3>(Bs, n, st);
+  case 4: return launch_batch_bm<BW, BH, 4>(Bs, n, st);
+  default: return cudaErrorNotSupported;
+  }
+}
+
 template <int BW, int BH>
 cudaError_t launch_size(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
   switch (a.inv.bm) {
@@ -199,6 +245,24 @@ cudaError_t launch_size(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark) {
 }
 
 }  // namespace
+
+cudaError_t launch_sweep_fast_batch(const SweepArgs* planes, int n, cudaStream_t st, cudaEvent_t mark) {
+  SweepBatch Bf, Bs, Bm;
+  if (!sweep_batches(planes, n, Bf, Bs, Bm, false))
+    return n < 1 || n > kMaxBatch ? cudaErrorInvalidValue : cudaErrorNotSupported;
+  int maxw = 0;
+  for (int i = 0; i < n; i++) maxw = std::max(maxw, planes[i].inv.g.W);
+  cudaError_t e;
+  switch (planes[0].inv.g.bw) {
+  case 8: e = launch_batch_size<8, 8>(Bs, n, st); break;
+  case 16: e = launch_batch_size<16, 16>(Bs, n, st); break;
+  case 32: e = launch_batch_size<32, 32>(Bs, n, st); break;
+  default: return cudaErrorNotSupported;
+  }
+  if (e != cudaSuccess) return e;
+  if (mark) cudaEventRecord(mark, st);
+  return launch_seam_merge_batch(Bm, n, maxw, planes[0].inv.g.bh / 2, st);
+}
 
 cudaError_t launch_seam_merge(const SweepArgs& a, cudaStream_t st) {
   if (a.segs < 2) return cudaSuccess;

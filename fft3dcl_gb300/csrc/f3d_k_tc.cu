@@ -1276,6 +1276,14 @@ cudaError_t launch_sweep_n(const SweepBatch& Bf, const SweepBatch& B, const Swee
 
 }  // namespace
 
+cudaError_t launch_seam_merge_batch(const SweepBatch& Bm, int n, int maxw, int ch, cudaStream_t st) {
+  if (Bm.cta0[n] == 0) return cudaSuccess;
+  dim3 grid((maxw + 255) / 256, ch, Bm.cta0[n]);
+  k_seam_merge_batch<<<grid, 256, 0, st>>>(Bm, ch);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sweep_tc_batch(const SweepArgs* planes, int n, const TcTune& t, cudaStream_t st,
                                   cudaEvent_t mark, cudaEvent_t after_filter) {
   SweepBatch Bf, B, Bm;

@@ -222,6 +222,11 @@ cudaError_t tc_graph_update(cudaGraphExec_t exec, cudaGraph_t graph, const TcFwd
 int tc_sweep_cells(int n);  // 7 for 32 x 32 blocks, 15 for 16 x 16
 constexpr int kTcSweepCtasPerSm = 3;
 cudaError_t launch_sweep_tc(const SweepArgs& a, cudaStream_t st, cudaEvent_t mark);
+// The fast form's fused sweeps of n planes (8x8 to 32x32 blocks, one
+// temporal mode) in one launch, then their seam rows in one more; `mark` is
+// recorded between the two.
+cudaError_t launch_sweep_fast_batch(const SweepArgs* planes, int n, cudaStream_t st, cudaEvent_t mark);
+cudaError_t launch_seam_merge_batch(const SweepBatch& Bm, int n, int maxw, int ch, cudaStream_t st);
 // Bytes of SweepArgs::img for this geometry and strip count.
 size_t tc_image_bytes(const Geo& g, int strips);
 cudaError_t launch_seam_merge(const SweepArgs& a, cudaStream_t st);

@@ -263,15 +263,20 @@ int f3d_denoise_noalloc(const f3d_script_params* sp, const f3d_plane_geom* geom,
  * engine given several times) with one launch per kernel: the forward
  * transform of each plane's entering frame, then filter, inverse and
  * overlap-add of each plane's window. The engines must run the fused
- * tensor-core form (F3D_FORM_TC, half overlap, 16x16 or 32x32 blocks) on one device
- * and one stream, with the same block size, overlap, window type, temporal
- * mode and sample format; plane sizes and bit depths may differ.
- * F3D_BATCH_GRAPH: each step shape is captured once as a CUDA graph and
- * replayed with its kernel nodes re-pointed at the step's buffers.
- * F3D_BATCH_AUTOTUNE: the first step in which every plane enters a frame
- * times the candidate launch shapes (forward CTAs per SM, filter-kernel
- * register budget) and keeps the fastest; results are cached per batch shape
- * for the process. Results are the same as the engines' own calls. */
+ * tensor-core form (F3D_FORM_TC, half overlap, 16x16 or 32x32 blocks), or
+ * all the fast form's fused sweep (F3D_FORM_FAST, half overlap, 8x8 to 32x32
+ * blocks: one forward launch per entering frame, the sweeps of all planes in
+ * one launch), on one device and one stream, with the same block size,
+ * overlap, window type, temporal mode and sample format; plane sizes and bit
+ * depths may differ.
+ * F3D_BATCH_GRAPH (tensor-core form): each step shape is captured once as a
+ * CUDA graph and replayed with its kernel nodes re-pointed at the step's
+ * buffers.
+ * F3D_BATCH_AUTOTUNE (tensor-core form): the first step in which every plane
+ * enters a frame times the candidate launch shapes (forward CTAs per SM,
+ * filter-kernel register budget) and keeps the fastest; results are cached
+ * per batch shape for the process. Results are the same as the engines' own
+ * calls. */
 #define F3D_BATCH_GRAPH 1
 #define F3D_BATCH_AUTOTUNE 2
 typedef struct f3d_batch f3d_batch;
@@ -295,8 +300,9 @@ int f3d_batch_tune(f3d_batch* b, int* fwd_ctas_per_sm, int* filter_minb);
 int f3d_batch_set_tune(f3d_batch* b, int fwd_ctas_per_sm, int filter_minb);
 /* Device times (ms) of the last step with outputs that ran outside a CUDA
  * graph (steps replayed as a graph are not timed): ms[0] the filter kernel,
- * ms[1] the inverse + overlap-add kernel and the seam merge. Waits for that
- * step. F3D_E_STATE when no such step ran. */
+ * ms[1] the inverse + overlap-add kernel and the seam merge (fast form:
+ * ms[0] the fused sweep, ms[1] the seam merge). Waits for that step.
+ * F3D_E_STATE when no such step ran. */
 int f3d_batch_last_kernel_ms(f3d_batch* b, float* ms);
 
 /* ---- Serving loop ----------------------------------------------------------

@@ -1,6 +1,7 @@
-"""Batches of tensor-core planes (f3d_batch_*): one launch per kernel for
-the planes of a YUV frame or of several streams, replayed as a CUDA graph and
-autotuned, give the same bits as each plane's own engine."""
+"""Batches of planes (f3d_batch_*): one launch per kernel for the planes of a
+YUV frame, of several streams or consecutive outputs of one plane, replayed
+as a CUDA graph and autotuned in the tensor-core form, launched directly in
+the fast form, give the same bits as each plane's own engine."""
 import numpy as np
 import pytest
 import torch
@@ -11,7 +12,7 @@ from fft3dcl_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def run_planes(planes, params, chroma_flags, bits, batch_flags, ahead=False, shape=None):
+def run_planes(planes, params, chroma_flags, bits, batch_flags, ahead=False, shape=None, form="tc"):
     """planes[i]: list of frames of plane i. Returns outputs per plane, by
     the batch when batch_flags is not None (with the launch shape pinned to
     `shape` when given), else by separate engines."""
@@ -20,7 +21,7 @@ def run_planes(planes, params, chroma_flags, bits, batch_flags, ahead=False, sha
     nfr = len(planes[0])
     ip = F.validate(planes[0][0].shape[1], planes[0][0].shape[0], bits, **params)
     bt, cur = ip.bt, ip.current
-    engines = [F.Engine(p[0].shape[1], p[0].shape[0], bits, chroma=c, form="tc", stream=st.cuda_stream, **params)
+    engines = [F.Engine(p[0].shape[1], p[0].shape[0], bits, chroma=c, form=form, stream=st.cuda_stream, **params)
                for p, c in zip(planes, chroma_flags)]
     src = [torch.from_numpy(np.stack(p)).to(dev) for p in planes]
     dst = [torch.empty(p[0].shape, dtype=src[i].dtype, device=dev) for i, p in enumerate(planes)]
@@ -252,7 +253,7 @@ def test_batch_rejects_mixed_forms():
             F.Batch([e1, e2])
 
 
-def consecutive_outputs(frames, bits, params, k, graph, shape=None, flags=0):
+def consecutive_outputs(frames, bits, params, k, graph, shape=None, flags=0, form="tc"):
     """The same engine k times in a batch: k consecutive outputs per step, the
     forwards of the next k frames concurrent with them. Returns the outputs
     and the batch's launch shape."""
@@ -261,7 +262,8 @@ def consecutive_outputs(frames, bits, params, k, graph, shape=None, flags=0):
     bt, cur = max(ip.bt, 1), ip.current
     dev = torch.device("cuda", 0)
     st = torch.cuda.Stream(device=dev)
-    e = F.Engine(w, h, bits, form="tc", stream=st.cuda_stream, flags=flags, **params)
+    e = F.Engine(w, h, bits, form=form, stream=st.cuda_stream, flags=flags, **params)
+    assert e.info().form == ["exact", "fast", "tc"].index(form)
     src = torch.from_numpy(np.stack(frames)).to(dev)
     dst = [torch.empty((h, w), dtype=src.dtype, device=dev) for _ in range(k)]
     b = F.Batch([e] * k, graph=graph, autotune=shape is None)
@@ -323,3 +325,29 @@ def test_consecutive_outputs_each_temporal_mode(bits, bt, k, graph, flags, extra
     got, _ = consecutive_outputs(frames, bits, params, k, graph, flags=flags)
     for n in range(len(frames)):
         np.testing.assert_array_equal(got[n], ref[n], err_msg=f"frame {n}")
+
+
+@pytest.mark.parametrize("k,graph", [(2, False), (4, True), (10, False)])
+def test_fast_batch_consecutive_outputs_equal_engine(k, graph):
+    # The fast form's batch: one forward launch per entering frame, the fused
+    # sweeps of the k outputs in one launch with their CTAs interleaved (the
+    # graph flag does not apply to it): the engine's own values bit for bit.
+    frames = synth.moving_rects(320, 192, 13, 71, lo=64, hi=940, noise=10.0, dtype=np.uint16, maxval=1023)
+    params = dict(sigma=3.0, bt=4, sharpen=0.3)
+    ref = F.FFT3DCL(frames, bits=10, form="fast", **params)
+    got, tune = consecutive_outputs(frames, 10, params, k, graph, form="fast")
+    assert not tune["tuned"]
+    for n in range(len(frames)):
+        np.testing.assert_array_equal(got[n], ref[n], err_msg=f"frame {n}")
+
+
+@pytest.mark.parametrize("bw", [8, 16, 32])
+def test_fast_batch_yuv_planes_equal_engines(bw):
+    y, u, v = yuv420(256, 160, 6, 81 + bw, 8)
+    params = dict(sigma=2.5, bt=3, bw=bw, bh=bw, sharpen=0.3)
+    ref, _ = run_planes([y, u, v], params, [False, True, True], 8, None, form="fast")
+    got, _ = run_planes([y, u, v], params, [False, True, True], 8, 0, ahead=True, form="fast")
+    for p in range(3):
+        for n in range(len(y)):
+            np.testing.assert_array_equal(got[p][n], ref[p][n], err_msg=f"plane {p} frame {n}")
+
