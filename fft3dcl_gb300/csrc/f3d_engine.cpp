@@ -929,11 +929,13 @@ int f3d_batch_create(f3d_engine* const* engines, int n, int flags, f3d_batch** o
     f3d_batch_destroy(b);
     return fail_thread(F3D_E_CUDA, "FFT3DCL: batch stream creation failed");
   }
-  std::lock_guard<std::mutex> lk(g_tune_mtx);
-  auto it = g_tune_cache.find(tune_key(b));
-  if (it != g_tune_cache.end()) {
-    b->tune = it->second;
-    b->tuned = true;
+  if (!b->fast) {  // the fast form has no launch shapes to tune
+    std::lock_guard<std::mutex> lk(g_tune_mtx);
+    auto it = g_tune_cache.find(tune_key(b));
+    if (it != g_tune_cache.end()) {
+      b->tune = it->second;
+      b->tuned = true;
+    }
   }
   *out = b;
   return F3D_OK;
