@@ -1,5 +1,5 @@
-// Host-side checks of the batched tensor-core launch plan
-// (fft3dcl_gb300/csrc/f3d_batch_plan.hpp): per-plane CTA prefixes, the
+// Host-side checks of the batched launch plan (tensor-core and fast forms,
+// fft3dcl_gb300/csrc/f3d_batch_plan.hpp): per-plane CTA prefixes, the
 // filter's runs of one geometry and its shifted-window bits, the batches
 // the plan refuses, and the autotuner's choice. Built and run by
 // tests/test_batch_plan_cpu.py; prints "ok" or the first failed check.
@@ -121,6 +121,29 @@ int main() {
     m[1] = plane(640, 360, 1, 0, 3, 1);
     m[1].img = nullptr;
     CHECK(!sweep_batches(m.data(), 2, Bf, Bs, Bm));
+  }
+  // The fast form's sweep plan: no tables or operand tiles needed, 8x8 to
+  // 32x32 blocks; the same prefixes and runs.
+  {
+    std::vector<SweepArgs> v;
+    for (int n = 0; n < 4; n++) {
+      SweepArgs a = plane(1920, 1080, 0, n, 4, 2);
+      a.tab = nullptr;
+      a.err = nullptr;
+      a.img = nullptr;
+      v.push_back(a);
+    }
+    CHECK(!sweep_batches(v.data(), 4, Bf, Bs, Bm));  // the tensor-core plan needs them
+    CHECK(sweep_batches(v.data(), 4, Bf, Bs, Bm, false));
+    CHECK(Bs.rlen[0] == 4 && Bs.shifted == 0xE);
+    for (int i = 0; i <= 4; i++) CHECK(Bs.cta0[i] == i * v[0].strips * v[0].segs);
+    for (auto& a : v) a.inv.g.bw = a.inv.g.bh = 8;
+    CHECK(sweep_batches(v.data(), 4, Bf, Bs, Bm, false));
+    CHECK(!sweep_batches(v.data(), 4, Bf, Bs, Bm));  // no 8x8 tensor-core sweep
+    v[1].inv.g.bw = v[1].inv.g.bh = 16;
+    CHECK(!sweep_batches(v.data(), 4, Bf, Bs, Bm, false));  // one block size per batch
+    v[1].inv.g.bw = v[1].inv.g.bh = 64;
+    CHECK(!sweep_batches(v.data(), 2, Bf, Bs, Bm, false));  // 64x64: no fused fast sweep
   }
   // Forward: block-group prefix, one group per 8 blocks of 32 x 32 (16 of
   // 16 x 16); the planes of a batch share the block size.
