@@ -1,7 +1,8 @@
 """ctypes bindings for the CPU oracle (test infrastructure only).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this package, and only as the checker. The product (the
+``bench.py`` import this package, and only as the oracle the CUDA path is
+compared with (or, for the CPU baseline, timed beside). The product (the
 ``fft3dcl_gb300`` package and its CUDA library) never imports it.
 
 Two libraries are bound here:

@@ -1,8 +1,8 @@
 /*
  * fft3d_oracle.c -- CPU oracle for the FFT3D block-FFT denoise path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA engine, never part of the
- * product. A C99 restatement of the fp32 CPU backend of HumbleUser33/FFT3dCL;
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA engine is compared with, never
+ * part of the product. A C99 restatement of the fp32 CPU backend of HumbleUser33/FFT3dCL;
  * every function names the reference file:line it follows. Build with
  * -ffp-contract=off (oracle/Makefile) so that no multiply-add is fused: the
  * reference is specified with MSVC /fp:precise (CMakeLists.txt:19-25).

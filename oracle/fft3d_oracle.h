@@ -1,9 +1,9 @@
 /*
  * fft3d_oracle.h -- CPU oracle for the FFT3D block-FFT denoise path.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker for the CUDA engine
- * (tests, the smoke check and the CPU baseline leg of the benchmark). The
- * product never links, loads or calls it.
+ * TEST INFRASTRUCTURE ONLY. This library is the oracle the CUDA engine is
+ * compared with (tests, the smoke check and the CPU baseline leg of the
+ * benchmark). The product never links, loads or calls it.
  *
  * It restates, in plain C99, the fp32 CPU backend of HumbleUser33/FFT3dCL
  * (src/cpu/reference.cpp, src/cpu/fft.cpp, src/cpu/tables.cpp, src/params.h)
