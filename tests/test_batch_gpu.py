@@ -341,10 +341,10 @@ def test_fast_batch_consecutive_outputs_equal_engine(k, graph):
         np.testing.assert_array_equal(got[n], ref[n], err_msg=f"frame {n}")
 
 
-@pytest.mark.parametrize("bw", [8, 16, 32])
-def test_fast_batch_yuv_planes_equal_engines(bw):
-    y, u, v = yuv420(256, 160, 6, 81 + bw, 8)
-    params = dict(sigma=2.5, bt=3, bw=bw, bh=bw, sharpen=0.3)
+@pytest.mark.parametrize("bw,bt", [(8, 3), (16, 3), (32, 3), (32, 1), (16, 4), (8, 2), (32, -1)])
+def test_fast_batch_yuv_planes_equal_engines(bw, bt):
+    y, u, v = yuv420(256, 160, 6, 81 + bw + bt, 8)
+    params = dict(sigma=2.5, bt=bt, bw=bw, bh=bw, sharpen=0.3)
     ref, _ = run_planes([y, u, v], params, [False, True, True], 8, None, form="fast")
     got, _ = run_planes([y, u, v], params, [False, True, True], 8, 0, ahead=True, form="fast")
     for p in range(3):
