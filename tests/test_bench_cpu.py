@@ -44,3 +44,13 @@ def test_algorithmic_bytes_of_the_other_workloads():
     u = oracle.Plane(960, 540, 8, chroma=True, **bench.YUV_PARAMS)
     sy, su = (p.nb * p.fbw * p.ip.bh * 8 for p in (y, u))
     assert bench.AB_YUV1080 == 2 * 1920 * 1080 + sy * 5 + 2 * (2 * 960 * 540 + su * 5) == 289187840
+
+
+def test_sections_are_the_extra_workloads():
+    # `--section NAME` runs one extra workload alone; the names are the keys
+    # the full line carries.
+    import inspect
+    src = inspect.getsource(bench.extra_section)
+    for name in bench.SECTIONS:
+        assert f'"{name}"' in src
+    assert set(bench.SECTIONS) == {"yuv1080p_all_planes", "gray8_640x360_bt3", "grays_1280x720_kalman_bw64"}
